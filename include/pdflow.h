@@ -1,0 +1,131 @@
+/*
+ * pdflow.h - C ABI of the GB300-native PD-Flow scene-flow solver.
+ *
+ * The entry points replace the host interface of the reference solver:
+ *   class PD_flow_opencv  (scene_flow_impair.h:53-115, scene_flow_impair.cpp:31-193)
+ *   class CSF_cuda host methods and bridges (pdflow_cudalib.h:125-134, :159-174)
+ * with plain pointers, sizes and integer status codes.  All image buffers use
+ * the reference's layout: column-major, rows contiguous, idx = v + u*height
+ * (scene_flow_impair.cpp:230-232).  Flow outputs are rows x cols, idx = v + u*rows
+ * (pdflow_cudalib.cu:239-244).  Axis convention of the flow (pdflow_cudalib.cu:1157-1159):
+ * dx = motion along the optical axis, dy = horizontal, dz = vertical, metres.
+ *
+ * Threading: a handle is not re-entrant; calls on one handle must be serialised
+ * by the caller (as the reference's object).  Distinct handles are independent.
+ * Every call returns PDFLOW_OK (0) or a negative pdflow_status.
+ */
+#ifndef PDFLOW_H
+#define PDFLOW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pdflow_status {
+    PDFLOW_OK = 0,
+    PDFLOW_ERR_ARG = -1,          /* bad size, null pointer or unsupported configuration */
+    PDFLOW_ERR_OOM = -2,          /* device arena could not be allocated / admission refused */
+    PDFLOW_ERR_CUDA = -3,         /* a CUDA runtime call failed (see pdflow_last_error) */
+    PDFLOW_ERR_STATE = -4,        /* call out of order (e.g. solve before two frames) */
+    PDFLOW_ERR_TIMEOUT = -5,      /* a bounded device-side wait gave up */
+    PDFLOW_ERR_NO_DEVICE = -6     /* no CUDA device of the supported architecture */
+} pdflow_status;
+
+/* Solver parameters.  Defaults (pdflow_default_params) are the reference's:
+ * lambda_i = 0.04, lambda_d = 0.35, mu = 75 (scene_flow_impair.cpp:67-69),
+ * fovh = 62.5 deg, fovv = 48.5 deg (:41-42), and the iteration schedule
+ * num_max_iter[i] = 100 at the finest level, -15 per coarser level (:46-52). */
+typedef struct pdflow_params {
+    float lambda_i;
+    float lambda_d;
+    float mu;
+    float fovh;                   /* radians */
+    float fovv;                   /* radians (kept for interface parity; unused by the solver) */
+    unsigned num_max_iter[6];     /* iterations per coarse-to-fine level, coarse -> fine */
+} pdflow_params;
+
+typedef struct pdflow_solver pdflow_solver;    /* opaque handle */
+
+/* Fills `p` with the reference defaults for `rows` (PD_flow_opencv ctor,
+ * scene_flow_impair.cpp:31-69). rows in {15,30,60,120,240,480}. */
+int pdflow_default_params(unsigned rows, pdflow_params* p);
+
+/* Creates a solver: replaces PD_flow_opencv::PD_flow_opencv + initializeCUDA
+ * (scene_flow_impair.cpp:31-77, :175-193) and CSF_cuda::readParameters +
+ * allocateDevMemory (pdflow_cudalib.cu:29-72, :176-193).
+ * rows in {15,30,60,120,240,480} (main_scene_flow_impair.cpp:83); image
+ * width x height is 640x480 or 320x240 (cam_mode 1 / 2, scene_flow_impair.cpp:182);
+ * cols = rows*4/3 must not exceed width.  `params` may be NULL for defaults.
+ * All device memory of the solver is allocated here, once. */
+int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_params* params,
+                  pdflow_solver** out);
+
+/* Releases the handle: replaces PD_flow_opencv::freeGPUMemory /
+ * CSF_cuda::freeDeviceMemory (scene_flow_impair.cpp:170-173, pdflow_cudalib.cu:249-288). */
+int pdflow_destroy(pdflow_solver* s);
+
+/* Pushes a new frame from the float staging buffers I, Z (host, width*height,
+ * column-major; Z in metres): replaces PD_flow_opencv::createImagePyramidGPU
+ * (scene_flow_impair.cpp:80-93), i.e. CSF_cuda::copyNewFrames + the Gaussian
+ * pyramid (pdflow_cudalib.cu:195-222, :1172-1184).  The previous frame becomes
+ * the old frame. */
+int pdflow_push_frame(pdflow_solver* s, const float* I, const float* Z);
+
+/* Same, from raw camera images as a PNG decoder returns them: row-major
+ * uint8 intensity and uint16 depth (metres * 5000), decoded on the device
+ * bit-exactly as the reference's host loop (scene_flow_impair.cpp:230-245,
+ * depth = uint16 * (float)(1/5000)). */
+int pdflow_push_frame_u16(pdflow_solver* s, const uint8_t* intensity, const uint16_t* depth);
+
+/* Same as pdflow_push_frame_u16 with device pointers (no host copy). */
+int pdflow_push_frame_u16_device(pdflow_solver* s, const uint8_t* d_intensity, const uint16_t* d_depth);
+
+/* Runs the coarse-to-fine solve on the last two pushed frames: replaces
+ * PD_flow_opencv::solveSceneFlowGPU (scene_flow_impair.cpp:95-168).  Asynchronous
+ * on the solver's stream; pdflow_read_flow or pdflow_synchronize waits. */
+int pdflow_solve(pdflow_solver* s);
+
+/* Copies the motion field (rows*cols floats each, column-major) to host
+ * memory: replaces CSF_cuda::copyMotionField (pdflow_cudalib.cu:239-244) and
+ * the public dxp/dyp/dzp buffers of PD_flow_opencv.  Blocks until the solve ends. */
+int pdflow_read_flow(pdflow_solver* s, float* dx, float* dy, float* dz);
+
+/* Device pointers of the solver's motion-field planes (valid until destroy). */
+int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, const float** dz);
+
+/* Copies pyramid level `level` (0 = full image resolution) of the old
+ * (frame = 0) or new (frame = 1) frame: intensity, depth and the
+ * back-projected xx, yy, each (height>>level)*(width>>level) floats,
+ * column-major.  Any pointer may be NULL.  Replaces the image part of
+ * CSF_cuda::copyAllSolutions (pdflow_cudalib.cu:224-237). */
+int pdflow_read_level_images(pdflow_solver* s, unsigned level, int frame, float* colour, float* depth, float* xx,
+                             float* yy);
+
+/* Waits for all work queued on the solver's stream. */
+int pdflow_synchronize(pdflow_solver* s);
+
+/* Uses `stream` (a cudaStream_t, or NULL for the solver's own stream) for all
+ * later work of this handle. */
+int pdflow_set_stream(pdflow_solver* s, void* stream);
+
+/* rows, cols, ctf_levels, pyr_levels, cam_mode of a handle (out may be NULL). */
+int pdflow_get_config(const pdflow_solver* s, unsigned* rows, unsigned* cols, unsigned* ctf_levels,
+                      unsigned* pyr_levels, unsigned* cam_mode);
+
+/* Selects the execution form of pdflow_solve: 0 = stream of kernels,
+ * 1 = the whole solve replayed as one captured CUDA graph (default). */
+int pdflow_set_graph_mode(pdflow_solver* s, int use_graph);
+
+/* Human-readable text of the last error on this thread. */
+const char* pdflow_last_error(void);
+
+/* Library version string. */
+const char* pdflow_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDFLOW_H */

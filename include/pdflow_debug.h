@@ -1,0 +1,38 @@
+/*
+ * pdflow_debug.h - inspection entry points of the GB300 PD-Flow solver, for
+ * stage-by-stage parity checks.  They have no production use and are not on
+ * the solve path.
+ */
+#ifndef PDFLOW_DEBUG_H
+#define PDFLOW_DEBUG_H
+
+#include "pdflow.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Receives one named plane (host memory, valid during the call). */
+typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const float* data, long n);
+
+/* Runs pdflow_solve kernel by kernel, synchronising after every stage and
+ * handing each intermediate to `fn` under the names of the reference's device
+ * arrays: per level `dct dcu dcv ddt ddu ddv mu ri rj ri_2 rj_2 du_prev dv_prev
+ * sigma_* tau_* init_*` after the set-up, `du_new ... pwv` after the
+ * iterations, `sat_du sat_dv sat_dw` after saturateVariables and
+ * `du_l dv_l dw_l` after the weighted median (the arrays the reference keeps
+ * in CSF_cuda, pdflow_cudalib.h:71-122).  The final flow equals pdflow_solve's. */
+int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
+
+/* The 3x3 weighted median of filterSolution (pdflow_cudalib.cu:1040-1148) on
+ * caller planes (device pointers, R*C floats, column-major).  `sel` (device,
+ * 3*R*C int32, may be NULL) receives, per component, the bracketing index the
+ * median picked (-1 where depth_old == 0). */
+int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const float* ddt, const float* du,
+                        const float* dv, const float* dw, float* du_l, float* dv_l, float* dw_l, int32_t* sel,
+                        void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDFLOW_DEBUG_H */

@@ -1,0 +1,140 @@
+// Inspection entry points (include/pdflow_debug.h) and the level-image
+// readback of include/pdflow.h.  Not on the solve path.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/pdflow.h"
+#include "../../include/pdflow_debug.h"
+#include "pdflow_internal.h"
+#include "pdflow_kernels.cuh"
+
+using namespace pdflow;
+
+namespace {
+
+int fail(const char* what, cudaError_t e)
+{
+    // Report through the solver's error slot by a failing no-op query.
+    std::fprintf(stderr, "pdflow debug: %s: %s\n", what, cudaGetErrorString(e));
+    return PDFLOW_ERR_CUDA;
+}
+
+struct Dumper {
+    pdflow_dump_fn fn;
+    void* ctx;
+    cudaStream_t st;
+    std::vector<float> buf;
+    int operator()(const char* name, int level, const float* dev, size_t n)
+    {
+        buf.resize(n);
+        cudaError_t e = cudaMemcpyAsync(buf.data(), dev, n * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail("dump copy", e);
+        fn(ctx, name, level, buf.data(), long(n));
+        return 0;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int pdflow_read_level_images(pdflow_solver* s, unsigned level, int frame, float* colour, float* depth, float* xx,
+                             float* yy)
+{
+    if (!s || level >= s->pyr_levels || (frame != 0 && frame != 1)) return PDFLOW_ERR_ARG;
+    const PyrLevel& P = s->pyr[frame ? s->new_slot : (s->new_slot ^ 1)][level];
+    const size_t n = (size_t(s->width) >> level) * (size_t(s->height) >> level);
+    const float* src[4] = {P.col, P.dep, P.xx, P.yy};
+    float* dst[4] = {colour, depth, xx, yy};
+    for (int a = 0; a < 4; ++a)
+        if (dst[a]) {
+            cudaError_t e = cudaMemcpyAsync(dst[a], src[a], n * 4, cudaMemcpyDeviceToHost, s->stream);
+            if (e != cudaSuccess) return fail("level image copy", e);
+        }
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? PDFLOW_OK : fail("synchronize", e);
+}
+
+int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
+{
+    if (!s || !fn) return PDFLOW_ERR_ARG;
+    if (s->frames < 2) return PDFLOW_ERR_STATE;
+    cudaStream_t st = s->stream;
+    Dumper dump{fn, ctx, st, {}};
+    Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
+    const int fn_ = s->new_slot, fo = fn_ ^ 1;
+    const LevelConsts& L = s->L;
+    const State& S = s->S;
+    for (unsigned i = 0; i < s->ctf_levels; ++i) {
+        unsigned li;
+        const LevelGeom g = level_geom(s, i, &li);
+        const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn_][li];
+        cudaError_t e = launch_level_init(g, i == 0, s->sol, o, n, L, S, st);
+        if (e == cudaSuccess) e = launch_im_gradients(g, n, L, st);
+        if (e == cudaSuccess) e = launch_warp_steps(g, o, n, L, p, st);
+        if (e != cudaSuccess) return fail("set-up launch", e);
+        const struct { const char* name; const float* ptr; } setup[] = {
+            {"dct", L.dct}, {"dcu", L.dcu}, {"dcv", L.dcv}, {"ddt", L.ddt}, {"ddu", L.ddu}, {"ddv", L.ddv},
+            {"mu", L.mu}, {"ri", L.ri}, {"rj", L.rj}, {"ri_2", L.ri2}, {"rj_2", L.rj2}, {"du_prev", L.du_prev},
+            {"dv_prev", L.dv_prev}, {"sigma_pd", L.spd}, {"sigma_puvx", L.spuvx}, {"sigma_puvy", L.spuvy},
+            {"sigma_pwx", L.spwx}, {"sigma_pwy", L.spwy}, {"tau_u", L.tu}, {"tau_v", L.tv}, {"tau_w", L.tw},
+            {"init_dw", S.dw}, {"init_dw_acc", S.dwa}, {"init_pd", S.pd}, {"init_puu", S.puu},
+            {"init_puv", S.puv}, {"init_pvu", S.pvu}, {"init_pvv", S.pvv}, {"init_pwu", S.pwu},
+            {"init_pwv", S.pwv}};
+        for (const auto& d : setup)
+            if (dump(d.name, int(i), d.ptr, g.N)) return PDFLOW_ERR_CUDA;
+        const unsigned iters = s->prm.num_max_iter[i];
+        for (unsigned it = 0; it < iters; ++it) {
+            e = launch_dual(g, L, S, p, st);
+            if (e == cudaSuccess) e = launch_primal(g, L, S, p, false, o.dep, st);
+            if (e != cudaSuccess) return fail("iteration launch", e);
+        }
+        const struct { const char* name; const float* ptr; } state[] = {
+            {"du_new", S.du}, {"dv_new", S.dv}, {"dw_new", S.dw}, {"du_acc", S.dua}, {"dv_acc", S.dva},
+            {"dw_acc", S.dwa}, {"pd", S.pd}, {"puu", S.puu}, {"puv", S.puv}, {"pvu", S.pvu}, {"pvv", S.pvv},
+            {"pwu", S.pwu}, {"pwv", S.pwv}};
+        for (const auto& d : state)
+            if (dump(d.name, int(i), d.ptr, g.N)) return PDFLOW_ERR_CUDA;
+        e = launch_saturate(g, L, S, o.dep, st);
+        if (e != cudaSuccess) return fail("saturate launch", e);
+        if (dump("sat_du", int(i), S.du, g.N) || dump("sat_dv", int(i), S.dv, g.N) ||
+            dump("sat_dw", int(i), S.dw, g.N))
+            return PDFLOW_ERR_CUDA;
+        e = launch_median(g, i + 1 == s->ctf_levels, o, L, S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st);
+        if (e != cudaSuccess) return fail("median launch", e);
+        if (dump("du_l", int(i), s->sol.du, g.N) || dump("dv_l", int(i), s->sol.dv, g.N) ||
+            dump("dw_l", int(i), s->sol.dw, g.N))
+            return PDFLOW_ERR_CUDA;
+    }
+    return PDFLOW_OK;
+}
+
+int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const float* ddt, const float* du,
+                        const float* dv, const float* dw, float* du_l, float* dv_l, float* dw_l, int32_t* sel,
+                        void* stream)
+{
+    if (!depth_old || !ddt || !du || !dv || !dw || !du_l || !dv_l || !dw_l || R < 2 || C < 2) return PDFLOW_ERR_ARG;
+    LevelGeom g{R, C, R * C};
+    PyrLevel o{nullptr, const_cast<float*>(depth_old), nullptr, nullptr};
+    LevelConsts L{};
+    L.ddt = const_cast<float*>(ddt);
+    State S{};
+    S.du = const_cast<float*>(du);
+    S.dv = const_cast<float*>(dv);
+    S.dw = const_cast<float*>(dw);
+    LevelSol out{};
+    out.du = du_l;
+    out.dv = dv_l;
+    out.dw = dw_l;
+    Params p{};
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_median(g, false, o, L, S, out, nullptr, nullptr, nullptr, p, sel, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? PDFLOW_OK : fail("stage median", e);
+}
+
+}  // extern "C"

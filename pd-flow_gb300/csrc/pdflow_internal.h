@@ -1,0 +1,39 @@
+// Internal definition of the solver handle (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/pdflow.h"
+#include "pdflow_kernels.cuh"
+
+struct pdflow_solver {
+    int device = 0;
+    unsigned rows = 0, cols = 0, width = 0, height = 0, cam_mode = 0, ctf_levels = 0, pyr_levels = 0;
+    pdflow_params prm{};
+    cudaStream_t stream = nullptr;       // stream used for all work of the handle
+    cudaStream_t own_stream = nullptr;
+    void* arena = nullptr;               // the one device allocation of the handle
+    size_t arena_bytes = 0;
+    // Pyramid of the two frames [slot][level]; `new_slot` holds the newest frame.
+    pdflow::PyrLevel pyr[2][8]{};
+    int new_slot = 1;
+    int frames = 0;                      // frames pushed (saturates at 2)
+    float* stage_I = nullptr;            // device staging of a float frame
+    float* stage_Z = nullptr;
+    uint8_t* stage_u8 = nullptr;         // device staging of a raw frame
+    uint16_t* stage_u16 = nullptr;
+    pdflow::LevelConsts L{};
+    pdflow::State S{};
+    pdflow::LevelSol sol{};
+    float* dx = nullptr;
+    float* dy = nullptr;
+    float* dz = nullptr;
+    int use_graph = 1;
+    cudaGraphExec_t solve_graph[2] = {nullptr, nullptr};  // one per old/new slot assignment
+};
+
+namespace pdflow {
+void carve_solver(pdflow_solver* s, char* base, size_t* used);
+int enqueue_pyramid(pdflow_solver* s, cudaStream_t st);
+int enqueue_solve(pdflow_solver* s, cudaStream_t st);
+LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image);
+}  // namespace pdflow

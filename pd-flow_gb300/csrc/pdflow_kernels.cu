@@ -1,0 +1,536 @@
+// Stage kernels of the PD-Flow solver on sm_103a.
+//
+// One thread per pixel, column-major planes (idx = v + u*R, rows contiguous,
+// so a warp reads 32 consecutive rows of one column: coalesced).  The per-level
+// set-up is fused into three kernels (init = zero/upsample + connectivity,
+// image gradients, warp + step sizes), an iteration is two kernels
+// (gradient+dual, divergence+primal; the reference uses four) and the last
+// primal kernel of a level also saturates; the weighted median and the motion
+// field are one kernel.  All per-pixel arithmetic lives in pdflow_math.cuh.
+#include "pdflow_kernels.cuh"
+#include "pdflow_math.cuh"
+
+namespace pdflow {
+
+namespace {
+
+constexpr unsigned kBlock = 256;
+
+__host__ __device__ inline unsigned blocks_for(unsigned n) { return (n + kBlock - 1) / kBlock; }
+
+// ---------------------------------------------------------------------------
+// Pyramid (computePyramidLevel, pdflow_cudalib.cu:331-434)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void write_xy(PyrLevel out, unsigned R, unsigned C, unsigned v, unsigned u,
+                                         unsigned idx, float depth, float fovh)
+{
+    const float inv_f_i = 2.f * tanf(0.5f * fovh) / float(C);
+    const float disp_u_i = 0.5f * (C - 1);
+    const float disp_v_i = 0.5f * (R - 1);
+    out.xx[idx] = (u - disp_u_i) * depth * inv_f_i;
+    out.yy[idx] = (v - disp_v_i) * depth * inv_f_i;
+}
+
+// Row-major uint8/uint16 camera images -> column-major level 0 (decode +
+// transpose through a 32x33 shared tile so that both sides are coalesced).
+__global__ void __launch_bounds__(1024) k_decode_u16(const uint8_t* __restrict__ img,
+                                                     const uint16_t* __restrict__ depth, unsigned W, unsigned H,
+                                                     PyrLevel out, float fovh)
+{
+    __shared__ float sc[32][33];
+    __shared__ float sz[32][33];
+    const unsigned x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    {
+        const unsigned x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+        if (x < W && y < H) {
+            const size_t i = (size_t)y * W + x;
+            sc[threadIdx.y][threadIdx.x] = float(img[i]);
+            sz[threadIdx.y][threadIdx.x] = decode_depth(depth[i]);
+        }
+    }
+    __syncthreads();
+    const unsigned v = y0 + threadIdx.x, u = x0 + threadIdx.y;  // writes walk along v
+    if (u < W && v < H) {
+        const unsigned idx = v + u * H;
+        const float z = sz[threadIdx.x][threadIdx.y];
+        out.col[idx] = sc[threadIdx.x][threadIdx.y];
+        out.dep[idx] = z;
+        write_xy(out, H, W, v, u, idx, z, fovh);
+    }
+}
+
+__global__ void k_pyr_level0(const float* __restrict__ I, const float* __restrict__ Z, unsigned R, unsigned C,
+                             PyrLevel out, float fovh)
+{
+    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= R * C) return;
+    const unsigned v = idx % R, u = idx / R;
+    out.col[idx] = I[idx];
+    const float z = Z[idx];
+    out.dep[idx] = z;
+    write_xy(out, R, C, v, u, idx, z, fovh);
+}
+
+__global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh)
+{
+    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= R * C) return;
+    const unsigned v = index % R, u = index / R;
+    const float max_depth_dif = 0.1f;
+    const float* __restrict__ cp = prev.col;
+    const float* __restrict__ dp = prev.dep;
+    float sumd = 0.f, sumc = 0.f, acu_weights_d = 0.f, acu_weights_c = 0.f;
+    const unsigned ind_cent_prev = 2 * v + 4 * u * R;
+    const float dcenter = dp[ind_cent_prev];
+    float dres, cres;
+    if ((v > 0) && (v < R - 1) && (u > 0) && (u < C - 1)) {
+#pragma unroll
+        for (int k = -2; k < 3; k++)
+#pragma unroll
+            for (int l = -2; l < 3; l++) {
+                const unsigned ind_loop_prev = 2 * v + k + 2 * (2 * u + l) * R;
+                const float gm = gmask(k, l);
+                sumc += gm * cp[ind_loop_prev];
+                const float d = dp[ind_loop_prev];
+                if ((d > 0.f) && (fabsf(d - dcenter) < max_depth_dif)) {
+                    const float aux_w = gm * (max_depth_dif - fabsf(d - dcenter));
+                    acu_weights_d += aux_w;
+                    sumd += aux_w * d;
+                }
+            }
+        dres = (sumd > 0.f) ? sumd / acu_weights_d : 0.f;
+        cres = sumc;
+    } else {
+        for (int k = -2; k < 3; k++)
+            for (int l = -2; l < 3; l++) {
+                const int indv = 2 * (int)v + k, indu = 2 * (int)u + l;
+                if ((indv >= 0) && (indv < 2 * (int)R) && (indu >= 0) && (indu < 2 * (int)C)) {
+                    const unsigned ind_loop_prev = 2 * v + k + 2 * (2 * u + l) * R;
+                    const float gm = gmask(k, l);
+                    sumc += gm * cp[ind_loop_prev];
+                    acu_weights_c += gm;
+                    const float d = dp[ind_loop_prev];
+                    if ((d > 0.f) && (fabsf(d - dp[ind_cent_prev]) < max_depth_dif)) {
+                        const float aux_w = gm * (max_depth_dif - fabsf(d - dp[ind_cent_prev]));
+                        acu_weights_d += aux_w;
+                        sumd += aux_w * d;
+                    }
+                }
+            }
+        cres = sumc / acu_weights_c;
+        dres = (sumd > 0.f) ? sumd / acu_weights_d : 0.f;
+    }
+    out.col[index] = cres;
+    out.dep[index] = dres;
+    write_xy(out, R, C, v, u, index, dres, fovh);
+}
+
+// ---------------------------------------------------------------------------
+// Level set-up
+// ---------------------------------------------------------------------------
+
+// assignZeros + upsampleCopy/upsampleFilterPrevSolution (pdflow_cudalib.cu:
+// 439-569) as a gather over the coarse solution (the zero-inserted taps
+// contribute exactly zero and are skipped), followed by computeRij (:725-779).
+__global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S)
+{
+    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = index % R, u = index / R;
+
+    float du = 0.f, dv = 0.f, dw = 0.f, pd = 0.f, puu = 0.f, puv = 0.f, pvu = 0.f, pvv = 0.f, pwu = 0.f, pwv = 0.f;
+    if (!first) {
+        const unsigned Rc = R / 2;
+        const bool inner = (v > 1) && (v < R - 2) && (u > 1) && (u < C - 2);
+        float acu_weight = 1.f;
+#pragma unroll
+        for (int k = -2; k < 3; k++)
+#pragma unroll
+            for (int l = -2; l < 3; l++) {
+                const int indv = (int)v + k, indu = (int)u + l;
+                const float gm4 = 4.f * gmask(k, l);
+                if ((indv < 0) || (indv >= (int)R) || (indu < 0) || (indu >= (int)C)) {
+                    acu_weight -= 0.25f * gm4;
+                    continue;
+                }
+                if ((indv & 1) || (indu & 1)) continue;  // zero-inserted tap
+                const unsigned ci = (unsigned)(indv >> 1) + (unsigned)(indu >> 1) * Rc;
+                du += gm4 * (2.f * cs.du[ci]);
+                dv += gm4 * (2.f * cs.dv[ci]);
+                dw += gm4 * cs.dw[ci];
+                pd += gm4 * cs.pd[ci];
+                puu += gm4 * cs.puu[ci];
+                puv += gm4 * cs.puv[ci];
+                pvu += gm4 * cs.pvu[ci];
+                pvv += gm4 * cs.pvv[ci];
+                pwu += gm4 * cs.pwu[ci];
+                pwv += gm4 * cs.pwv[ci];
+            }
+        if (!inner) {
+            const float inv_acu_weight = fdividef(1.f, acu_weight);
+            du *= inv_acu_weight;
+            dv *= inv_acu_weight;
+            dw *= inv_acu_weight;
+            pd *= inv_acu_weight;
+            puu *= inv_acu_weight;
+            puv *= inv_acu_weight;
+            pvu *= inv_acu_weight;
+            pvv *= inv_acu_weight;
+            pwu *= inv_acu_weight;
+            pwv *= inv_acu_weight;
+        }
+    }
+    L.du_prev[index] = du;
+    L.dv_prev[index] = dv;
+    S.du[index] = 0.f;
+    S.dv[index] = 0.f;
+    S.dw[index] = dw;
+    S.dua[index] = 0.f;
+    S.dva[index] = 0.f;
+    S.dwa[index] = dw;
+    S.pd[index] = pd;
+    S.puu[index] = puu;
+    S.puv[index] = puv;
+    S.pvu[index] = pvu;
+    S.pvv[index] = pvv;
+    S.pwu[index] = pwu;
+    S.pwv[index] = pwv;
+
+    // computeRij
+    float dxu = 0.f, dzu = 0.f, dxu_2 = 0.f, dzu_2 = 0.f, dyv = 0.f, dzv = 0.f, dyv_2 = 0.f, dzv_2 = 0.f;
+    if (u != C - 1) {
+        dxu = o.xx[index + R] - o.xx[index];
+        dzu = o.dep[index + R] - o.dep[index];
+        dxu_2 = n.xx[index + R] - n.xx[index];
+        dzu_2 = n.dep[index + R] - n.dep[index];
+    }
+    if (v != R - 1) {
+        dyv = o.yy[index + 1] - o.yy[index];
+        dzv = o.dep[index + 1] - o.dep[index];
+        dyv_2 = n.yy[index + 1] - n.yy[index];
+        dzv_2 = n.dep[index + 1] - n.dep[index];
+    }
+    L.ri[index] = rfac(dxu, dzu);
+    L.rj[index] = rfac(dyv, dzv);
+    L.ri2[index] = rfac(dxu_2, dzu_2);
+    L.rj2[index] = rfac(dyv_2, dzv_2);
+}
+
+// computeImGradients (pdflow_cudalib.cu:574-627) on the new frame.
+__global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
+{
+    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = index % R, u = index / R;
+    const float* __restrict__ c = n.col;
+    const float* __restrict__ d = n.dep;
+    const float* __restrict__ ri2 = L.ri2;
+    const float* __restrict__ rj2 = L.rj2;
+    if (u == 0) {
+        L.dcu_aux[index] = c[index + R] - c[index];
+        L.ddu_aux[index] = d[index + R] - d[index];
+    } else if (u == C - 1) {
+        L.dcu_aux[index] = c[index] - c[index - R];
+        L.ddu_aux[index] = d[index] - d[index - R];
+    } else {
+        L.dcu_aux[index] = (ri2[index] * (c[index + R] - c[index]) + ri2[index - R] * (c[index] - c[index - R])) /
+                           (ri2[index] + ri2[index - R]);
+        if (d[index] > 0.f)
+            L.ddu_aux[index] = (ri2[index] * (d[index + R] - d[index]) + ri2[index - R] * (d[index] - d[index - R])) /
+                               (ri2[index] + ri2[index - R]);
+        else
+            L.ddu_aux[index] = 0.f;
+    }
+    if (v == 0) {
+        L.dcv_aux[index] = c[index + 1] - c[index];
+        L.ddv_aux[index] = d[index + 1] - d[index];
+    } else if (v == R - 1) {
+        L.dcv_aux[index] = c[index] - c[index - 1];
+        L.ddv_aux[index] = d[index] - d[index - 1];
+    } else {
+        L.dcv_aux[index] = (rj2[index] * (c[index + 1] - c[index]) + rj2[index - 1] * (c[index] - c[index - 1])) /
+                           (rj2[index] + rj2[index - 1]);
+        if (d[index] > 0.f)
+            L.ddv_aux[index] = (rj2[index] * (d[index + 1] - d[index]) + rj2[index - 1] * (d[index] - d[index - 1])) /
+                               (rj2[index] + rj2[index - 1]);
+        else
+            L.ddv_aux[index] = 0.f;
+    }
+}
+
+// performWarping (pdflow_cudalib.cu:629-652) + computeMu/computeStepSizes (:781-808).
+__global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p)
+{
+    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = index % R, u = index / R;
+    const float ind_uf = float(u) + L.du_prev[index];
+    const float ind_vf = float(v) + L.dv_prev[index];
+    const float dct = interp(n.col, R, C, ind_uf, ind_vf) - o.col[index];
+    const float dcu = interp(L.dcu_aux, R, C, ind_uf, ind_vf);
+    const float dcv = interp(L.dcv_aux, R, C, ind_uf, ind_vf);
+    const float wz = interp_depth(n.dep, R, C, ind_uf, ind_vf);
+    const float ddt = (wz > 0.f) ? wz - o.dep[index] : 0.f;
+    const float ddu = interp(L.ddu_aux, R, C, ind_uf, ind_vf);
+    const float ddv = interp(L.ddv_aux, R, C, ind_uf, ind_vf);
+    L.dct[index] = dct;
+    L.dcu[index] = dcu;
+    L.dcv[index] = dcv;
+    L.ddt[index] = ddt;
+    L.ddu[index] = ddu;
+    L.ddv[index] = ddv;
+    const float ri = L.ri[index], rj = L.rj[index];
+    const float ri_m = (u > 0) ? L.ri[index - R] : 0.f;
+    const float rj_m = (v > 0) ? L.rj[index - 1] : 0.f;
+    const Steps s = mu_and_steps(p.mu, p.lambda_i, p.lambda_d, ddu, ddv, ddt, ri, rj, ri_m, rj_m, u > 0, v > 0);
+    L.mu[index] = s.mu;
+    L.spd[index] = s.spd;
+    L.spuvx[index] = s.spuvx;
+    L.spuvy[index] = s.spuvy;
+    L.spwx[index] = s.spwx;
+    L.spwy[index] = s.spwy;
+    L.tu[index] = s.tu;
+    L.tv[index] = s.tv;
+    L.tw[index] = s.tw;
+}
+
+// ---------------------------------------------------------------------------
+// Iteration kernels
+// ---------------------------------------------------------------------------
+__global__ void k_dual(LevelGeom g, LevelConsts L, State S, Params p)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = i % R, u = i / R;
+    const bool lu = (u == C - 1), lv = (v == R - 1);
+    const unsigned iu = lu ? i : i + R, iv = lv ? i : i + 1;
+    Duals d{S.pd[i], S.puu[i], S.puv[i], S.pvu[i], S.pvv[i], S.pwu[i], S.pwv[i]};
+    dual_update(d, L.spd[i], L.spuvx[i], L.spuvy[i], L.spwx[i], L.spwy[i], L.mu[i], L.ddt[i], L.ddu[i], L.ddv[i],
+                p.lambda_i, p.lambda_d, L.ri[i], L.rj[i], S.dua[i], S.dva[i], S.dwa[i], L.du_prev[i], L.dv_prev[i],
+                S.dua[iu], S.dva[iu], S.dwa[iu], L.du_prev[iu], L.dv_prev[iu], S.dua[iv], S.dva[iv], S.dwa[iv],
+                L.du_prev[iv], L.dv_prev[iv], lu, lv);
+    S.pd[i] = d.pd;
+    S.puu[i] = d.puu;
+    S.puv[i] = d.puv;
+    S.pvu[i] = d.pvu;
+    S.pvv[i] = d.pvv;
+    S.pwu[i] = d.pwu;
+    S.pwv[i] = d.pwv;
+}
+
+__global__ void k_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = i % R, u = i / R;
+    const bool fu = (u == 0), lu = (u == C - 1), fv = (v == 0), lv = (v == R - 1);
+    const unsigned im = fu ? i : i - R, jm = fv ? i : i - 1;
+    const float ri = L.ri[i], rj = L.rj[i], ri_m = L.ri[im], rj_m = L.rj[jm];
+    const float divu = divergence(ri, ri_m, rj, rj_m, S.puu[i], S.puu[im], S.puv[i], S.puv[jm], fu, lu, fv, lv);
+    const float divv = divergence(ri, ri_m, rj, rj_m, S.pvu[i], S.pvu[im], S.pvv[i], S.pvv[jm], fu, lu, fv, lv);
+    const float divw = divergence(ri, ri_m, rj, rj_m, S.pwu[i], S.pwu[im], S.pwv[i], S.pwv[jm], fu, lu, fv, lv);
+    float du = S.du[i], dv = S.dv[i], dw = S.dw[i], dua, dva, dwa;
+    primal_update(du, dv, dw, dua, dva, dwa, L.tu[i], L.tv[i], L.tw[i], L.mu[i], L.ddu[i], L.ddv[i], S.pd[i],
+                  p.lambda_i, p.lambda_d, divu, divv, divw, L.dct[i], L.dcu[i], L.dcv[i]);
+    if (last) {
+        saturate(du, dv, dw, L.du_prev[i], L.dv_prev[i], depth_old[i]);
+    } else {
+        S.dua[i] = dua;
+        S.dva[i] = dva;
+        S.dwa[i] = dwa;
+    }
+    S.du[i] = du;
+    S.dv[i] = dv;
+    S.dw[i] = dw;
+}
+
+// saturateVariables alone, for a level scheduled with zero iterations.
+__global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    float du = S.du[i], dv = S.dv[i], dw = S.dw[i];
+    saturate(du, dv, dw, L.du_prev[i], L.dv_prev[i], depth_old[i]);
+    S.du[i] = du;
+    S.dv[i] = dv;
+    S.dw[i] = dw;
+}
+
+// ---------------------------------------------------------------------------
+// filterSolution (pdflow_cudalib.cu:1040-1148) + computeMotionField (:1150-1167)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bubble_sort(float* f, float* w, unsigned n)
+{
+    bool go_on = true;
+    while (go_on) {
+        go_on = false;
+        for (unsigned i = 1; i < n; i++)
+            if (f[i - 1] > f[i]) {
+                float t = f[i - 1]; f[i - 1] = f[i]; f[i] = t;
+                t = w[i - 1]; w[i - 1] = w[i]; w[i] = t;
+                go_on = true;
+            }
+    }
+}
+
+__device__ __forceinline__ float median_pick(const float* f, const float* cum, float pres_med, int32_t* cont_out)
+{
+    unsigned cont = 0;
+    while (pres_med > cum[cont]) cont++;
+    *cont_out = (int32_t)cont;
+    if (cont == 0) return f[0];
+    const unsigned ind_r = cont, ind_l = cont - 1;
+    return ((cum[ind_r] - pres_med) * f[ind_l] + (pres_med - cum[ind_l]) * f[ind_r]) / (cum[ind_r] - cum[ind_l]);
+}
+
+__global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, LevelSol out, float* dx,
+                         float* dy, float* dz, Params p, int32_t* sel)
+{
+    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = index % R, u = index / R;
+    const float depth_old = o.dep[index];
+    const float kd = 5.f, kddt = 10.f;
+    float ru, rv, rw;
+    if (depth_old > 0.f) {
+        float fu[9], fv[9], fw[9], wu[9], wv[9], ww[9];
+        unsigned point_count = 9, vi = 0;
+        for (int k = -1; k < 2; k++)
+            for (int l = -1; l < 2; l++) {
+                const int indr = (int)v + k, indc = (int)u + l;
+                if ((indr < 0) || (indr >= (int)R) || (indc < 0) || (indc >= (int)C)) {
+                    point_count--;
+                    continue;
+                }
+                const int j = (int)index + l * (int)R + k;
+                const float pres = 1.f / (1.f + kd * powf(depth_old - o.dep[j], 2.f) + kddt * powf(L.ddt[j], 2.f));
+                fu[vi] = S.du[j]; wu[vi] = pres;
+                fv[vi] = S.dv[j]; wv[vi] = pres;
+                fw[vi] = S.dw[j]; ww[vi] = pres;
+                vi++;
+            }
+        bubble_sort(fu, wu, point_count);
+        bubble_sort(fv, wv, point_count);
+        bubble_sort(fw, ww, point_count);
+        float cu[9], cv[9], cw[9];
+        cu[0] = wu[0]; cv[0] = wv[0]; cw[0] = ww[0];
+        for (unsigned q = 1; q < point_count; q++) {
+            cu[q] = cu[q - 1] + wu[q];
+            cv[q] = cv[q - 1] + wv[q];
+            cw[q] = cw[q - 1] + ww[q];
+        }
+        const float pres_med = 0.5f * cu[point_count - 1];
+        int32_t c0, c1, c2;
+        ru = median_pick(fu, cu, pres_med, &c0);
+        rv = median_pick(fv, cv, pres_med, &c1);
+        rw = median_pick(fw, cw, pres_med, &c2);
+        if (sel) { sel[index] = c0; sel[g.N + index] = c1; sel[2 * g.N + index] = c2; }
+    } else {
+        ru = S.du[index];
+        rv = S.dv[index];
+        rw = S.dw[index];
+        if (sel) { sel[index] = -1; sel[g.N + index] = -1; sel[2 * g.N + index] = -1; }
+    }
+    out.du[index] = ru;
+    out.dv[index] = rv;
+    out.dw[index] = rw;
+    if (!out.pd) return;  // stage form: no duals to carry
+    out.pd[index] = S.pd[index];
+    out.puu[index] = S.puu[index];
+    out.puv[index] = S.puv[index];
+    out.pvu[index] = S.pvu[index];
+    out.pvv[index] = S.pvv[index];
+    out.pwu[index] = S.pwu[index];
+    out.pwv[index] = S.pwv[index];
+    if (finest) {
+        const float inv_f = 2.f * tanf(0.5f * p.fovh) / float(p.cols);
+        if (depth_old > 0) {
+            dx[index] = rw;
+            dy[index] = depth_old * ru * inv_f + rw * o.xx[index] / depth_old;
+            dz[index] = depth_old * rv * inv_f + rw * o.yy[index] / depth_old;
+        } else {
+            dx[index] = 0.f;
+            dy[index] = 0.f;
+            dz[index] = 0.f;
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
+                              float fovh, cudaStream_t st)
+{
+    dim3 grid((W + 31) / 32, (H + 31) / 32), block(32, 32);
+    k_decode_u16<<<grid, block, 0, st>>>(img, depth, W, H, out, fovh);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pyr_level0(const float* I, const float* Z, unsigned R, unsigned C, PyrLevel out, float fovh,
+                              cudaStream_t st)
+{
+    k_pyr_level0<<<blocks_for(R * C), kBlock, 0, st>>>(I, Z, R, C, out, fovh);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, cudaStream_t st)
+{
+    k_pyr_down<<<blocks_for(R * C), kBlock, 0, st>>>(prev, R, C, out, fovh);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel old_l, PyrLevel new_l,
+                              LevelConsts L, State S, cudaStream_t st)
+{
+    k_level_init<<<blocks_for(g.N), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st)
+{
+    k_im_gradients<<<blocks_for(g.N), kBlock, 0, st>>>(g, new_l, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p, cudaStream_t st)
+{
+    k_warp_steps<<<blocks_for(g.N), kBlock, 0, st>>>(g, old_l, new_l, L, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dual(LevelGeom g, LevelConsts L, State S, Params p, cudaStream_t st)
+{
+    k_dual<<<blocks_for(g.N), kBlock, 0, st>>>(g, L, S, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old,
+                          cudaStream_t st)
+{
+    k_primal<<<blocks_for(g.N), kBlock, 0, st>>>(g, L, S, p, last, depth_old);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old, cudaStream_t st)
+{
+    k_saturate<<<blocks_for(g.N), kBlock, 0, st>>>(g, L, S, depth_old);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out, float* dx,
+                          float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st)
+{
+    k_median<<<blocks_for(g.N), kBlock, 0, st>>>(g, finest, old_l, L, S, out, dx, dy, dz, p, sel);
+    return cudaGetLastError();
+}
+
+}  // namespace pdflow

@@ -1,0 +1,367 @@
+// Host side of the solver: one device arena per handle, the coarse-to-fine
+// schedule of PD_flow_opencv::solveSceneFlowGPU (scene_flow_impair.cpp:95-168),
+// CUDA-graph replay of the whole solve, and the C ABI of include/pdflow.h.
+//
+// Unlike the reference, which calls cudaMalloc ~60 times and cudaFree ~55
+// times per pyramid level (pdflow_cudalib.cu:74-162, :290-326), every device
+// buffer is carved once from a single allocation at create time, so a solve
+// issues no allocation, no host synchronisation and (in graph mode) one launch.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/pdflow.h"
+#include "pdflow_internal.h"
+#include "pdflow_kernels.cuh"
+
+using namespace pdflow;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char* what, cudaError_t e = cudaSuccess)
+{
+    char buf[512];
+    if (e != cudaSuccess)
+        std::snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    else
+        std::snprintf(buf, sizeof buf, "%s", what);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(call, what)                                  \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return set_error(PDFLOW_ERR_CUDA, what, _e); \
+    } while (0)
+
+unsigned log2u(unsigned x)
+{
+    unsigned l = 0;
+    while (x > 1) { x >>= 1; ++l; }
+    return l;
+}
+
+bool valid_rows(unsigned r)
+{
+    return r == 15 || r == 30 || r == 60 || r == 120 || r == 240 || r == 480;
+}
+
+// Bump allocator over the arena (256-byte aligned planes).
+struct Carver {
+    char* base;
+    size_t off;
+    bool dry;
+    float* plane(size_t n)
+    {
+        off = (off + 255) & ~size_t(255);
+        float* p = dry ? nullptr : reinterpret_cast<float*>(base + off);
+        off += n * sizeof(float);
+        return p;
+    }
+    void* bytes(size_t n)
+    {
+        off = (off + 255) & ~size_t(255);
+        void* p = dry ? nullptr : base + off;
+        off += n;
+        return p;
+    }
+};
+
+}  // namespace
+
+namespace pdflow {
+
+void carve_solver(pdflow_solver* s, char* base, size_t* used)
+{
+    Carver cv{base, 0, base == nullptr};
+    const size_t Nimg = size_t(s->width) * s->height;
+    for (int f = 0; f < 2; ++f)
+        for (unsigned l = 0; l < s->pyr_levels; ++l) {
+            const size_t n = Nimg >> (2 * l);
+            s->pyr[f][l] = PyrLevel{cv.plane(n), cv.plane(n), cv.plane(n), cv.plane(n)};
+        }
+    s->stage_I = cv.plane(Nimg);
+    s->stage_Z = cv.plane(Nimg);
+    s->stage_u8 = static_cast<uint8_t*>(cv.bytes(Nimg));
+    s->stage_u16 = static_cast<uint16_t*>(cv.bytes(Nimg * 2));
+    const size_t N = size_t(s->rows) * s->cols;
+    LevelConsts& L = s->L;
+    float** lp[] = {&L.ri, &L.rj, &L.ri2, &L.rj2, &L.dcu_aux, &L.dcv_aux, &L.ddu_aux, &L.ddv_aux, &L.dct,
+                    &L.dcu, &L.dcv, &L.ddt, &L.ddu, &L.ddv, &L.mu, &L.du_prev, &L.dv_prev, &L.spd, &L.spuvx,
+                    &L.spuvy, &L.spwx, &L.spwy, &L.tu, &L.tv, &L.tw};
+    for (float** p : lp) *p = cv.plane(N);
+    State& S = s->S;
+    float** sp[] = {&S.du, &S.dv, &S.dw, &S.dua, &S.dva, &S.dwa, &S.pd, &S.puu, &S.puv, &S.pvu, &S.pvv, &S.pwu,
+                    &S.pwv};
+    for (float** p : sp) *p = cv.plane(N);
+    LevelSol& O = s->sol;
+    float** op[] = {&O.du, &O.dv, &O.dw, &O.pd, &O.puu, &O.puv, &O.pvu, &O.pvv, &O.pwu, &O.pwv};
+    for (float** p : op) *p = cv.plane(N);
+    s->dx = cv.plane(N);
+    s->dy = cv.plane(N);
+    s->dz = cv.plane(N);
+    *used = cv.off;
+}
+
+int enqueue_pyramid(pdflow_solver* s, cudaStream_t st)
+{
+    const int f = s->new_slot;
+    for (unsigned l = 1; l < s->pyr_levels; ++l) {
+        const unsigned Cl = 640 / (s->cam_mode << l), Rl = 480 / (s->cam_mode << l);
+        CUDA_TRY(launch_pyr_down(s->pyr[f][l - 1], Rl, Cl, s->pyr[f][l], s->prm.fovh, st), "pyramid launch");
+    }
+    return PDFLOW_OK;
+}
+
+LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image)
+{
+    const unsigned sdiv = 1u << (s->ctf_levels - (i + 1));
+    const unsigned Ci = s->cols / sdiv, Ri = s->rows / sdiv;
+    if (level_image) *level_image = s->ctf_levels - i + log2u(s->width / s->cols) - 1;
+    return LevelGeom{Ri, Ci, Ri * Ci};
+}
+
+// The kernel sequence of one solve (scene_flow_impair.cpp:103-167), for the
+// current old/new slot assignment.
+int enqueue_solve(pdflow_solver* s, cudaStream_t st)
+{
+    Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
+    const int fn = s->new_slot, fo = fn ^ 1;
+    for (unsigned i = 0; i < s->ctf_levels; ++i) {
+        unsigned li;
+        const LevelGeom g = level_geom(s, i, &li);
+        const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];
+        CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st), "level init launch");
+        CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
+        CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
+        const unsigned iters = s->prm.num_max_iter[i];
+        for (unsigned it = 0; it < iters; ++it) {
+            CUDA_TRY(launch_dual(g, s->L, s->S, p, st), "dual launch");
+            CUDA_TRY(launch_primal(g, s->L, s->S, p, it + 1 == iters, o.dep, st), "primal launch");
+        }
+        if (iters == 0) CUDA_TRY(launch_saturate(g, s->L, s->S, o.dep, st), "saturate launch");
+        CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, s->S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
+                 "median launch");
+    }
+    return PDFLOW_OK;
+}
+
+}  // namespace pdflow
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int pdflow_default_params(unsigned rows, pdflow_params* p)
+{
+    if (!p) return set_error(PDFLOW_ERR_ARG, "null params");
+    if (!valid_rows(rows)) return set_error(PDFLOW_ERR_ARG, "rows must be one of 15,30,60,120,240,480");
+    const unsigned ctf = log2u(rows / 15) + 1;
+    for (int i = 5; i >= 0; --i)
+        p->num_max_iter[i] = (i >= int(ctf) - 1) ? 100u : p->num_max_iter[i + 1] - 15u;
+    p->lambda_i = 0.04f;
+    p->lambda_d = 0.35f;
+    p->mu = 75.f;
+    p->fovh = float(M_PI * 62.5 / 180.0);
+    p->fovv = float(M_PI * 48.5 / 180.0);
+    return PDFLOW_OK;
+}
+
+int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_params* params, pdflow_solver** out)
+{
+    if (!out) return set_error(PDFLOW_ERR_ARG, "null output handle");
+    *out = nullptr;
+    if (!valid_rows(rows)) return set_error(PDFLOW_ERR_ARG, "rows must be one of 15,30,60,120,240,480");
+    if (!((width == 640 && height == 480) || (width == 320 && height == 240)))
+        return set_error(PDFLOW_ERR_ARG, "image must be 640x480 or 320x240");
+    const unsigned cols = rows * 320 / 240;
+    if (cols > width) return set_error(PDFLOW_ERR_ARG, "rows exceed the image resolution");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+    if (!(prop.major == 10 && prop.minor == 3))
+        return set_error(PDFLOW_ERR_NO_DEVICE, "this library is built for sm_103a (GB300) only");
+
+    pdflow_solver* s = new (std::nothrow) pdflow_solver();
+    if (!s) return set_error(PDFLOW_ERR_OOM, "host allocation");
+    s->device = dev;
+    s->rows = rows;
+    s->cols = cols;
+    s->width = width;
+    s->height = height;
+    s->cam_mode = (height == 240) ? 2u : 1u;
+    s->ctf_levels = log2u(rows / 15) + 1;
+    s->pyr_levels = log2u(width / cols) + s->ctf_levels;
+    if (params) s->prm = *params;
+    else pdflow_default_params(rows, &s->prm);
+    s->use_graph = 1;
+    size_t bytes = 0;
+    carve_solver(s, nullptr, &bytes);
+    cudaError_t e = cudaMalloc(&s->arena, bytes);
+    if (e != cudaSuccess) {
+        delete s;
+        return set_error(PDFLOW_ERR_OOM, "arena allocation", e);
+    }
+    s->arena_bytes = bytes;
+    carve_solver(s, static_cast<char*>(s->arena), &bytes);
+    e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->arena, 0, s->arena_bytes, s->own_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->own_stream);
+    if (e != cudaSuccess) {
+        cudaFree(s->arena);
+        if (s->own_stream) cudaStreamDestroy(s->own_stream);
+        delete s;
+        return set_error(PDFLOW_ERR_CUDA, "stream / arena init", e);
+    }
+    s->stream = s->own_stream;
+    *out = s;
+    return PDFLOW_OK;
+}
+
+int pdflow_destroy(pdflow_solver* s)
+{
+    if (!s) return PDFLOW_OK;
+    cudaStreamSynchronize(s->stream);
+    for (int k = 0; k < 2; ++k)
+        if (s->solve_graph[k]) cudaGraphExecDestroy(s->solve_graph[k]);
+    cudaFree(s->arena);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+    return PDFLOW_OK;
+}
+
+int pdflow_push_frame(pdflow_solver* s, const float* I, const float* Z)
+{
+    if (!s || !I || !Z) return set_error(PDFLOW_ERR_ARG, "null argument");
+    const size_t n = size_t(s->width) * s->height;
+    s->new_slot ^= 1;  // copyNewFrames pointer swap (pdflow_cudalib.cu:203-221)
+    CUDA_TRY(cudaMemcpyAsync(s->stage_I, I, n * 4, cudaMemcpyHostToDevice, s->stream), "H2D intensity");
+    CUDA_TRY(cudaMemcpyAsync(s->stage_Z, Z, n * 4, cudaMemcpyHostToDevice, s->stream), "H2D depth");
+    CUDA_TRY(launch_pyr_level0(s->stage_I, s->stage_Z, s->height, s->width, s->pyr[s->new_slot][0], s->prm.fovh,
+                               s->stream),
+             "level-0 launch");
+    int rc = enqueue_pyramid(s, s->stream);
+    if (rc) return rc;
+    if (s->frames < 2) ++s->frames;
+    return PDFLOW_OK;
+}
+
+int pdflow_push_frame_u16_device(pdflow_solver* s, const uint8_t* d_intensity, const uint16_t* d_depth)
+{
+    if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    s->new_slot ^= 1;
+    CUDA_TRY(launch_decode_u16(d_intensity, d_depth, s->width, s->height, s->pyr[s->new_slot][0], s->prm.fovh,
+                               s->stream),
+             "decode launch");
+    int rc = enqueue_pyramid(s, s->stream);
+    if (rc) return rc;
+    if (s->frames < 2) ++s->frames;
+    return PDFLOW_OK;
+}
+
+int pdflow_push_frame_u16(pdflow_solver* s, const uint8_t* intensity, const uint16_t* depth)
+{
+    if (!s || !intensity || !depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    const size_t n = size_t(s->width) * s->height;
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u8, intensity, n, cudaMemcpyHostToDevice, s->stream), "H2D intensity");
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u16, depth, n * 2, cudaMemcpyHostToDevice, s->stream), "H2D depth");
+    return pdflow_push_frame_u16_device(s, s->stage_u8, s->stage_u16);
+}
+
+int pdflow_solve(pdflow_solver* s)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (s->frames < 2) return set_error(PDFLOW_ERR_STATE, "solve needs two pushed frames");
+    if (!s->use_graph) return enqueue_solve(s, s->stream);
+    cudaGraphExec_t& ge = s->solve_graph[s->new_slot];
+    if (!ge) {
+        cudaStream_t cap;
+        CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        int rc = PDFLOW_OK;
+        if (e == cudaSuccess) {
+            rc = enqueue_solve(s, cap);
+            cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess && rc == PDFLOW_OK) e = cudaGraphInstantiate(&ge, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cap);
+        if (rc != PDFLOW_OK) return rc;
+        if (e != cudaSuccess) {
+            ge = nullptr;
+            return set_error(PDFLOW_ERR_CUDA, "solve graph capture", e);
+        }
+    }
+    CUDA_TRY(cudaGraphLaunch(ge, s->stream), "solve graph launch");
+    return PDFLOW_OK;
+}
+
+int pdflow_read_flow(pdflow_solver* s, float* dx, float* dy, float* dz)
+{
+    if (!s || !dx || !dy || !dz) return set_error(PDFLOW_ERR_ARG, "null argument");
+    const size_t n = size_t(s->rows) * s->cols * 4;
+    CUDA_TRY(cudaMemcpyAsync(dx, s->dx, n, cudaMemcpyDeviceToHost, s->stream), "D2H dx");
+    CUDA_TRY(cudaMemcpyAsync(dy, s->dy, n, cudaMemcpyDeviceToHost, s->stream), "D2H dy");
+    CUDA_TRY(cudaMemcpyAsync(dz, s->dz, n, cudaMemcpyDeviceToHost, s->stream), "D2H dz");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
+    return PDFLOW_OK;
+}
+
+int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, const float** dz)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (dx) *dx = s->dx;
+    if (dy) *dy = s->dy;
+    if (dz) *dz = s->dz;
+    return PDFLOW_OK;
+}
+
+int pdflow_synchronize(pdflow_solver* s)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
+    return PDFLOW_OK;
+}
+
+int pdflow_set_stream(pdflow_solver* s, void* stream)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    s->stream = stream ? static_cast<cudaStream_t>(stream) : s->own_stream;
+    return PDFLOW_OK;
+}
+
+int pdflow_get_config(const pdflow_solver* s, unsigned* rows, unsigned* cols, unsigned* ctf_levels,
+                      unsigned* pyr_levels, unsigned* cam_mode)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (rows) *rows = s->rows;
+    if (cols) *cols = s->cols;
+    if (ctf_levels) *ctf_levels = s->ctf_levels;
+    if (pyr_levels) *pyr_levels = s->pyr_levels;
+    if (cam_mode) *cam_mode = s->cam_mode;
+    return PDFLOW_OK;
+}
+
+int pdflow_set_graph_mode(pdflow_solver* s, int use_graph)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    s->use_graph = use_graph ? 1 : 0;
+    return PDFLOW_OK;
+}
+
+const char* pdflow_last_error(void) { return g_last_error.c_str(); }
+
+const char* pdflow_version(void) { return "pdflow-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,224 @@
+"""ctypes binding of libpdflow_gb300.so (the C ABI of include/pdflow.h).
+
+The library is the only compute path: there is no CPU fallback.  Loading it
+fails loudly (ExtensionMissing) when it has not been built, and a solver
+cannot be created without a GB300 (sm_103) device.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_STATE, ERR_TIMEOUT, ERR_NO_DEVICE = 0, -1, -2, -3, -4, -5, -6
+
+
+class ExtensionMissing(RuntimeError):
+    pass
+
+
+class PDFlowError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what} failed with status {code}: {last_error()}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    """pdflow_params (include/pdflow.h)."""
+    _fields_ = [("lambda_i", ctypes.c_float), ("lambda_d", ctypes.c_float), ("mu", ctypes.c_float),
+                ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
+
+
+DUMP_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int,
+                           ctypes.POINTER(ctypes.c_float), ctypes.c_long)
+
+_lib = None
+vp = ctypes.c_void_p
+u32 = ctypes.c_uint
+
+_SIGNATURES = {
+    "pdflow_default_params": (ctypes.c_int, [u32, ctypes.POINTER(Params)]),
+    "pdflow_create": (ctypes.c_int, [u32, u32, u32, ctypes.POINTER(Params), ctypes.POINTER(vp)]),
+    "pdflow_destroy": (ctypes.c_int, [vp]),
+    "pdflow_push_frame": (ctypes.c_int, [vp, vp, vp]),
+    "pdflow_push_frame_u16": (ctypes.c_int, [vp, vp, vp]),
+    "pdflow_push_frame_u16_device": (ctypes.c_int, [vp, vp, vp]),
+    "pdflow_solve": (ctypes.c_int, [vp]),
+    "pdflow_read_flow": (ctypes.c_int, [vp, vp, vp, vp]),
+    "pdflow_flow_device": (ctypes.c_int, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]),
+    "pdflow_read_level_images": (ctypes.c_int, [vp, u32, ctypes.c_int, vp, vp, vp, vp]),
+    "pdflow_synchronize": (ctypes.c_int, [vp]),
+    "pdflow_set_stream": (ctypes.c_int, [vp, vp]),
+    "pdflow_get_config": (ctypes.c_int, [vp] + [ctypes.POINTER(u32)] * 5),
+    "pdflow_set_graph_mode": (ctypes.c_int, [vp, ctypes.c_int]),
+    "pdflow_last_error": (ctypes.c_char_p, []),
+    "pdflow_version": (ctypes.c_char_p, []),
+    "pdflow_debug_solve": (ctypes.c_int, [vp, DUMP_FN, vp]),
+    "pdflow_stage_median": (ctypes.c_int, [u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+}
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Loads the in-tree library (building it first if asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise ExtensionMissing(f"{path} is not built; run __graft_entry__.build() or python -m pdflow.build")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def last_error() -> str:
+    if _lib is None:
+        return ""
+    s = _lib.pdflow_last_error()
+    return s.decode() if s else ""
+
+
+def check(code: int, what: str):
+    if code != OK:
+        raise PDFlowError(code, what)
+
+
+def default_params(rows: int) -> Params:
+    p = Params()
+    check(load().pdflow_default_params(rows, ctypes.byref(p)), "pdflow_default_params")
+    return p
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Solver:
+    """One PD-Flow solver (C handle).  Method names follow the reference's
+    PD_flow_opencv (scene_flow_impair.h:53-115): construct, initializeCUDA,
+    createImagePyramidGPU / loadRGBDFrames, solveSceneFlowGPU, dxp/dyp/dzp,
+    freeGPUMemory."""
+
+    def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
+                 use_graph: bool = True):
+        self.rows, self.width, self.height = rows, width, height
+        self.cols = rows * 320 // 240
+        self.params = params
+        self._h = None
+        self._use_graph = use_graph
+        self.dxp = self.dyp = self.dzp = None
+
+    # -- reference-shaped API --------------------------------------------------
+    def initializeCUDA(self):
+        lib = load()
+        h = ctypes.c_void_p()
+        p = ctypes.byref(self.params) if self.params is not None else None
+        check(lib.pdflow_create(self.rows, self.width, self.height, p, ctypes.byref(h)), "pdflow_create")
+        self._h = h
+        check(lib.pdflow_set_graph_mode(h, int(self._use_graph)), "pdflow_set_graph_mode")
+        n = self.rows * self.cols
+        self.dxp, self.dyp, self.dzp = (np.zeros(n, np.float32) for _ in range(3))
+        return self
+
+    def createImagePyramidGPU(self, I: np.ndarray, Z: np.ndarray):
+        """Push a frame given as the reference's float staging buffers (column-major)."""
+        I = np.ascontiguousarray(I, np.float32).ravel()
+        Z = np.ascontiguousarray(Z, np.float32).ravel()
+        if I.size != self.width * self.height or Z.size != I.size:
+            raise ValueError("frame size does not match the solver")
+        check(load().pdflow_push_frame(self._h, _ptr(I), _ptr(Z)), "pdflow_push_frame")
+
+    def push_raw(self, intensity: np.ndarray, depth: np.ndarray):
+        """Push a frame as row-major uint8 intensity / uint16 depth (decoded on the GPU)."""
+        i8 = np.ascontiguousarray(intensity, np.uint8)
+        z16 = np.ascontiguousarray(depth, np.uint16)
+        if i8.shape != (self.height, self.width) or z16.shape != i8.shape:
+            raise ValueError("frame size does not match the solver")
+        check(load().pdflow_push_frame_u16(self._h, _ptr(i8), _ptr(z16)), "pdflow_push_frame_u16")
+
+    def loadRGBDFrames(self, i1, z1, i2, z2):
+        """Push two raw frames (the reference loads two PNGs, scene_flow_impair.cpp:218-277)."""
+        self.push_raw(i1, z1)
+        self.push_raw(i2, z2)
+        return True
+
+    def solveSceneFlowGPU(self, read_back: bool = True):
+        check(load().pdflow_solve(self._h), "pdflow_solve")
+        if read_back:
+            self.read_flow()
+
+    def read_flow(self):
+        check(load().pdflow_read_flow(self._h, _ptr(self.dxp), _ptr(self.dyp), _ptr(self.dzp)),
+              "pdflow_read_flow")
+        return self.dxp, self.dyp, self.dzp
+
+    def freeGPUMemory(self):
+        if self._h is not None:
+            load().pdflow_destroy(self._h)
+            self._h = None
+
+    # -- extras ----------------------------------------------------------------
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self):
+        check(load().pdflow_synchronize(self._h), "pdflow_synchronize")
+
+    def config(self):
+        vals = [u32() for _ in range(5)]
+        check(load().pdflow_get_config(self._h, *[ctypes.byref(v) for v in vals]), "pdflow_get_config")
+        return dict(zip(("rows", "cols", "ctf_levels", "pyr_levels", "cam_mode"), (v.value for v in vals)))
+
+    def level_images(self, level: int, frame: int):
+        w, h = self.width >> level, self.height >> level
+        out = [np.zeros(w * h, np.float32) for _ in range(4)]
+        check(load().pdflow_read_level_images(self._h, level, frame, *[_ptr(a) for a in out]),
+              "pdflow_read_level_images")
+        return dict(zip(("colour", "depth", "xx", "yy"), out))
+
+    def debug_solve(self):
+        store = {}
+
+        def _cb(ctx, name, level, ptr, n):
+            store[(name.decode(), level)] = np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+        cb = DUMP_FN(_cb)
+        check(load().pdflow_debug_solve(self._h, cb, None), "pdflow_debug_solve")
+        self.read_flow()
+        return store
+
+    def __enter__(self):
+        if self._h is None:
+            self.initializeCUDA()
+        return self
+
+    def __exit__(self, *exc):
+        self.freeGPUMemory()
+
+    def __del__(self):
+        try:
+            self.freeGPUMemory()
+        except Exception:
+            pass
+
+
+PD_flow = Solver
