@@ -83,6 +83,7 @@ typedef struct {
     unsigned rows, cols, width, height, cam_mode, ctf_levels, pyr_levels;
     unsigned num_max_iter[6];
     float g_mask[25];
+    unsigned long long iter_dump_mask;   /* bit k: dump level-0 state after iteration k+1 */
     char err[256];
 } refh;
 
@@ -104,6 +105,8 @@ static unsigned get_u32(const refh* h, unsigned off) { unsigned v; memcpy(&v, h-
 static unsigned log2u(unsigned x) { unsigned l = 0; while (x > 1) { x >>= 1; ++l; } return l; }
 
 const char* refh_error(refh* h) { return h ? h->err : "null handle"; }
+
+void refh_set_iter_dump_mask(refh* h, unsigned long long mask) { if (h) h->iter_dump_mask = mask; }
 
 static int launch(refh* h, int which, CUdeviceptr dobj, const unsigned* level)
 {
@@ -310,6 +313,20 @@ int refh_solve(refh* h, float* dxp, float* dyp, float* dzp, refh_dump_fn dump, v
             if ((rc = launch(h, K_DUAL, d, 0))) return rc;
             if ((rc = launch(h, K_DIV, d, 0))) return rc;
             if ((rc = launch(h, K_PRIM, d, 0))) return rc;
+            /* optional per-iteration snapshots of the coarsest level's state */
+            if (dump && i == 0 && it + 1 < h->num_max_iter[i] && it < 64 && ((h->iter_dump_mask >> it) & 1ull)) {
+                static const char* nm[] = {"du_new", "dv_new", "dw_new", "du_acc", "dv_acc", "dw_acc", "pd", "puu",
+                                           "puv", "pvu", "pvv", "pwu", "pwv"};
+                const unsigned offs[] = {CSF_OFF_du_new_dev, CSF_OFF_dv_new_dev, CSF_OFF_dw_new_dev,
+                                         CSF_OFF_du_acc_dev, CSF_OFF_dv_acc_dev, CSF_OFF_dw_acc_dev, CSF_OFF_pd_dev,
+                                         CSF_OFF_puu_dev, CSF_OFF_puv_dev, CSF_OFF_pvu_dev, CSF_OFF_pvv_dev,
+                                         CSF_OFF_pwu_dev, CSF_OFF_pwv_dev};
+                for (unsigned q = 0; q < sizeof(offs) / sizeof(offs[0]); ++q) {
+                    char name[48];
+                    snprintf(name, sizeof name, "it%u_%s", it + 1, nm[q]);
+                    if ((rc = dump_dev(h, dump, ctx, name, (int)i, get_ptr(h, offs[q]), n))) return rc;
+                }
+            }
         }
         if (dump) {
             static const char* nm[] = {"du_new", "dv_new", "dw_new", "du_acc", "dv_acc", "dw_acc", "pd", "puu",

@@ -50,6 +50,7 @@ def lib():
         _lib.refh_destroy.argtypes = [ctypes.c_void_p]
         _lib.refh_error.argtypes = [ctypes.c_void_p]
         _lib.refh_error.restype = ctypes.c_char_p
+        _lib.refh_set_iter_dump_mask.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong]
     return _lib
 
 
@@ -86,6 +87,10 @@ class RefSolver:
         dx, dy, dz = (np.zeros(n, np.float32) for _ in range(3))
         self._check(L.refh_solve(self.h, dx, dy, dz, cb, None), "solve")
         return (dx, dy, dz, store) if dump else (dx, dy, dz)
+
+    def set_iter_dump_mask(self, mask: int):
+        """Dump the coarsest level's state after iteration k+1 for every set bit k."""
+        lib().refh_set_iter_dump_mask(self.h, mask)
 
     def time_pairs(self, I1, Z1, I2, Z2, reps: int) -> float:
         n = self.rows * self.cols

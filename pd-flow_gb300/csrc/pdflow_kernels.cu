@@ -24,11 +24,9 @@ __host__ __device__ inline unsigned blocks_for(unsigned n) { return (n + kBlock 
 __device__ __forceinline__ void write_xy(PyrLevel out, unsigned R, unsigned C, unsigned v, unsigned u,
                                          unsigned idx, float depth, float fovh)
 {
-    const float inv_f_i = 2.f * tanf(0.5f * fovh) / float(C);
-    const float disp_u_i = 0.5f * (C - 1);
-    const float disp_v_i = 0.5f * (R - 1);
-    out.xx[idx] = (u - disp_u_i) * depth * inv_f_i;
-    out.yy[idx] = (v - disp_v_i) * depth * inv_f_i;
+    const float inv_f_i = inv_focal(fovh, C);
+    out.xx[idx] = backproject(u, C, depth, inv_f_i);
+    out.yy[idx] = backproject(v, R, depth, inv_f_i);
 }
 
 // Row-major uint8/uint16 camera images -> column-major level 0 (decode +
@@ -83,6 +81,8 @@ __global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, 
     const unsigned ind_cent_prev = 2 * v + 4 * u * R;
     const float dcenter = dp[ind_cent_prev];
     float dres, cres;
+    // sumc and sumd fuse their products; the depth weight is added after
+    // rounding (acu_weights_d += aux_w), as in the reference build.
     if ((v > 0) && (v < R - 1) && (u > 0) && (u < C - 1)) {
 #pragma unroll
         for (int k = -2; k < 3; k++)
@@ -90,15 +90,16 @@ __global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, 
             for (int l = -2; l < 3; l++) {
                 const unsigned ind_loop_prev = 2 * v + k + 2 * (2 * u + l) * R;
                 const float gm = gmask(k, l);
-                sumc += gm * cp[ind_loop_prev];
+                sumc = fm(gm, cp[ind_loop_prev], sumc);
                 const float d = dp[ind_loop_prev];
-                if ((d > 0.f) && (fabsf(d - dcenter) < max_depth_dif)) {
-                    const float aux_w = gm * (max_depth_dif - fabsf(d - dcenter));
-                    acu_weights_d += aux_w;
-                    sumd += aux_w * d;
+                const float ad = fabsf(sub(d, dcenter));
+                if ((d > 0.f) && (ad < max_depth_dif)) {
+                    const float aux_w = mul(gm, sub(max_depth_dif, ad));
+                    acu_weights_d = add(acu_weights_d, aux_w);
+                    sumd = fm(aux_w, d, sumd);
                 }
             }
-        dres = (sumd > 0.f) ? sumd / acu_weights_d : 0.f;
+        dres = (sumd > 0.f) ? qt(sumd, acu_weights_d) : 0.f;
         cres = sumc;
     } else {
         for (int k = -2; k < 3; k++)
@@ -107,18 +108,19 @@ __global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, 
                 if ((indv >= 0) && (indv < 2 * (int)R) && (indu >= 0) && (indu < 2 * (int)C)) {
                     const unsigned ind_loop_prev = 2 * v + k + 2 * (2 * u + l) * R;
                     const float gm = gmask(k, l);
-                    sumc += gm * cp[ind_loop_prev];
-                    acu_weights_c += gm;
+                    sumc = fm(gm, cp[ind_loop_prev], sumc);
+                    acu_weights_c = add(acu_weights_c, gm);
                     const float d = dp[ind_loop_prev];
-                    if ((d > 0.f) && (fabsf(d - dp[ind_cent_prev]) < max_depth_dif)) {
-                        const float aux_w = gm * (max_depth_dif - fabsf(d - dp[ind_cent_prev]));
-                        acu_weights_d += aux_w;
-                        sumd += aux_w * d;
+                    const float ad = fabsf(sub(d, dcenter));
+                    if ((d > 0.f) && (ad < max_depth_dif)) {
+                        const float aux_w = mul(gm, sub(max_depth_dif, ad));
+                        acu_weights_d = add(acu_weights_d, aux_w);
+                        sumd = fm(aux_w, d, sumd);
                     }
                 }
             }
-        cres = sumc / acu_weights_c;
-        dres = (sumd > 0.f) ? sumd / acu_weights_d : 0.f;
+        cres = qt(sumc, acu_weights_c);
+        dres = (sumd > 0.f) ? qt(sumd, acu_weights_d) : 0.f;
     }
     out.col[index] = cres;
     out.dep[index] = dres;
@@ -149,36 +151,36 @@ __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, P
 #pragma unroll
             for (int l = -2; l < 3; l++) {
                 const int indv = (int)v + k, indu = (int)u + l;
-                const float gm4 = 4.f * gmask(k, l);
+                const float gm4 = mul(4.f, gmask(k, l));
                 if ((indv < 0) || (indv >= (int)R) || (indu < 0) || (indu >= (int)C)) {
-                    acu_weight -= 0.25f * gm4;
+                    acu_weight = sub(acu_weight, mul(0.25f, gm4));
                     continue;
                 }
                 if ((indv & 1) || (indu & 1)) continue;  // zero-inserted tap
                 const unsigned ci = (unsigned)(indv >> 1) + (unsigned)(indu >> 1) * Rc;
-                du += gm4 * (2.f * cs.du[ci]);
-                dv += gm4 * (2.f * cs.dv[ci]);
-                dw += gm4 * cs.dw[ci];
-                pd += gm4 * cs.pd[ci];
-                puu += gm4 * cs.puu[ci];
-                puv += gm4 * cs.puv[ci];
-                pvu += gm4 * cs.pvu[ci];
-                pvv += gm4 * cs.pvv[ci];
-                pwu += gm4 * cs.pwu[ci];
-                pwv += gm4 * cs.pwv[ci];
+                du = fm(gm4, mul(2.f, cs.du[ci]), du);
+                dv = fm(gm4, mul(2.f, cs.dv[ci]), dv);
+                dw = fm(gm4, cs.dw[ci], dw);
+                pd = fm(gm4, cs.pd[ci], pd);
+                puu = fm(gm4, cs.puu[ci], puu);
+                puv = fm(gm4, cs.puv[ci], puv);
+                pvu = fm(gm4, cs.pvu[ci], pvu);
+                pvv = fm(gm4, cs.pvv[ci], pvv);
+                pwu = fm(gm4, cs.pwu[ci], pwu);
+                pwv = fm(gm4, cs.pwv[ci], pwv);
             }
         if (!inner) {
             const float inv_acu_weight = fdividef(1.f, acu_weight);
-            du *= inv_acu_weight;
-            dv *= inv_acu_weight;
-            dw *= inv_acu_weight;
-            pd *= inv_acu_weight;
-            puu *= inv_acu_weight;
-            puv *= inv_acu_weight;
-            pvu *= inv_acu_weight;
-            pvv *= inv_acu_weight;
-            pwu *= inv_acu_weight;
-            pwv *= inv_acu_weight;
+            du = mul(du, inv_acu_weight);
+            dv = mul(dv, inv_acu_weight);
+            dw = mul(dw, inv_acu_weight);
+            pd = mul(pd, inv_acu_weight);
+            puu = mul(puu, inv_acu_weight);
+            puv = mul(puv, inv_acu_weight);
+            pvu = mul(pvu, inv_acu_weight);
+            pvv = mul(pvv, inv_acu_weight);
+            pwu = mul(pwu, inv_acu_weight);
+            pwv = mul(pwv, inv_acu_weight);
         }
     }
     L.du_prev[index] = du;
@@ -200,16 +202,16 @@ __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, P
     // computeRij
     float dxu = 0.f, dzu = 0.f, dxu_2 = 0.f, dzu_2 = 0.f, dyv = 0.f, dzv = 0.f, dyv_2 = 0.f, dzv_2 = 0.f;
     if (u != C - 1) {
-        dxu = o.xx[index + R] - o.xx[index];
-        dzu = o.dep[index + R] - o.dep[index];
-        dxu_2 = n.xx[index + R] - n.xx[index];
-        dzu_2 = n.dep[index + R] - n.dep[index];
+        dxu = sub(o.xx[index + R], o.xx[index]);
+        dzu = sub(o.dep[index + R], o.dep[index]);
+        dxu_2 = sub(n.xx[index + R], n.xx[index]);
+        dzu_2 = sub(n.dep[index + R], n.dep[index]);
     }
     if (v != R - 1) {
-        dyv = o.yy[index + 1] - o.yy[index];
-        dzv = o.dep[index + 1] - o.dep[index];
-        dyv_2 = n.yy[index + 1] - n.yy[index];
-        dzv_2 = n.dep[index + 1] - n.dep[index];
+        dyv = sub(o.yy[index + 1], o.yy[index]);
+        dzv = sub(o.dep[index + 1], o.dep[index]);
+        dyv_2 = sub(n.yy[index + 1], n.yy[index]);
+        dzv_2 = sub(n.dep[index + 1], n.dep[index]);
     }
     L.ri[index] = rfac(dxu, dzu);
     L.rj[index] = rfac(dyv, dzv);
@@ -229,34 +231,26 @@ __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
     const float* __restrict__ ri2 = L.ri2;
     const float* __restrict__ rj2 = L.rj2;
     if (u == 0) {
-        L.dcu_aux[index] = c[index + R] - c[index];
-        L.ddu_aux[index] = d[index + R] - d[index];
+        L.dcu_aux[index] = sub(c[index + R], c[index]);
+        L.ddu_aux[index] = sub(d[index + R], d[index]);
     } else if (u == C - 1) {
-        L.dcu_aux[index] = c[index] - c[index - R];
-        L.ddu_aux[index] = d[index] - d[index - R];
+        L.dcu_aux[index] = sub(c[index], c[index - R]);
+        L.ddu_aux[index] = sub(d[index], d[index - R]);
     } else {
-        L.dcu_aux[index] = (ri2[index] * (c[index + R] - c[index]) + ri2[index - R] * (c[index] - c[index - R])) /
-                           (ri2[index] + ri2[index - R]);
-        if (d[index] > 0.f)
-            L.ddu_aux[index] = (ri2[index] * (d[index + R] - d[index]) + ri2[index - R] * (d[index] - d[index - R])) /
-                               (ri2[index] + ri2[index - R]);
-        else
-            L.ddu_aux[index] = 0.f;
+        L.dcu_aux[index] = wgrad(ri2[index], ri2[index - R], c[index + R], c[index], c[index - R]);
+        L.ddu_aux[index] = (d[index] > 0.f) ? wgrad(ri2[index], ri2[index - R], d[index + R], d[index], d[index - R])
+                                            : 0.f;
     }
     if (v == 0) {
-        L.dcv_aux[index] = c[index + 1] - c[index];
-        L.ddv_aux[index] = d[index + 1] - d[index];
+        L.dcv_aux[index] = sub(c[index + 1], c[index]);
+        L.ddv_aux[index] = sub(d[index + 1], d[index]);
     } else if (v == R - 1) {
-        L.dcv_aux[index] = c[index] - c[index - 1];
-        L.ddv_aux[index] = d[index] - d[index - 1];
+        L.dcv_aux[index] = sub(c[index], c[index - 1]);
+        L.ddv_aux[index] = sub(d[index], d[index - 1]);
     } else {
-        L.dcv_aux[index] = (rj2[index] * (c[index + 1] - c[index]) + rj2[index - 1] * (c[index] - c[index - 1])) /
-                           (rj2[index] + rj2[index - 1]);
-        if (d[index] > 0.f)
-            L.ddv_aux[index] = (rj2[index] * (d[index + 1] - d[index]) + rj2[index - 1] * (d[index] - d[index - 1])) /
-                               (rj2[index] + rj2[index - 1]);
-        else
-            L.ddv_aux[index] = 0.f;
+        L.dcv_aux[index] = wgrad(rj2[index], rj2[index - 1], c[index + 1], c[index], c[index - 1]);
+        L.ddv_aux[index] = (d[index] > 0.f) ? wgrad(rj2[index], rj2[index - 1], d[index + 1], d[index], d[index - 1])
+                                            : 0.f;
     }
 }
 
@@ -267,13 +261,13 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
     if (index >= g.N) return;
     const unsigned R = g.R, C = g.C;
     const unsigned v = index % R, u = index / R;
-    const float ind_uf = float(u) + L.du_prev[index];
-    const float ind_vf = float(v) + L.dv_prev[index];
-    const float dct = interp(n.col, R, C, ind_uf, ind_vf) - o.col[index];
+    const float ind_uf = add(float(u), L.du_prev[index]);
+    const float ind_vf = add(float(v), L.dv_prev[index]);
+    const float dct = sub(interp(n.col, R, C, ind_uf, ind_vf), o.col[index]);
     const float dcu = interp(L.dcu_aux, R, C, ind_uf, ind_vf);
     const float dcv = interp(L.dcv_aux, R, C, ind_uf, ind_vf);
     const float wz = interp_depth(n.dep, R, C, ind_uf, ind_vf);
-    const float ddt = (wz > 0.f) ? wz - o.dep[index] : 0.f;
+    const float ddt = (wz > 0.f) ? sub(wz, o.dep[index]) : 0.f;
     const float ddu = interp(L.ddu_aux, R, C, ind_uf, ind_vf);
     const float ddv = interp(L.ddv_aux, R, C, ind_uf, ind_vf);
     L.dct[index] = dct;
@@ -384,8 +378,7 @@ __device__ __forceinline__ float median_pick(const float* f, const float* cum, f
     while (pres_med > cum[cont]) cont++;
     *cont_out = (int32_t)cont;
     if (cont == 0) return f[0];
-    const unsigned ind_r = cont, ind_l = cont - 1;
-    return ((cum[ind_r] - pres_med) * f[ind_l] + (pres_med - cum[ind_l]) * f[ind_r]) / (cum[ind_r] - cum[ind_l]);
+    return median_lerp(cum[cont], cum[cont - 1], pres_med, f[cont - 1], f[cont]);
 }
 
 __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, LevelSol out, float* dx,
@@ -396,7 +389,6 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     const unsigned R = g.R, C = g.C;
     const unsigned v = index % R, u = index / R;
     const float depth_old = o.dep[index];
-    const float kd = 5.f, kddt = 10.f;
     float ru, rv, rw;
     if (depth_old > 0.f) {
         float fu[9], fv[9], fw[9], wu[9], wv[9], ww[9];
@@ -409,7 +401,7 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
                     continue;
                 }
                 const int j = (int)index + l * (int)R + k;
-                const float pres = 1.f / (1.f + kd * powf(depth_old - o.dep[j], 2.f) + kddt * powf(L.ddt[j], 2.f));
+                const float pres = median_weight(depth_old, o.dep[j], L.ddt[j]);
                 fu[vi] = S.du[j]; wu[vi] = pres;
                 fv[vi] = S.dv[j]; wv[vi] = pres;
                 fw[vi] = S.dw[j]; ww[vi] = pres;
@@ -421,11 +413,11 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
         float cu[9], cv[9], cw[9];
         cu[0] = wu[0]; cv[0] = wv[0]; cw[0] = ww[0];
         for (unsigned q = 1; q < point_count; q++) {
-            cu[q] = cu[q - 1] + wu[q];
-            cv[q] = cv[q - 1] + wv[q];
-            cw[q] = cw[q - 1] + ww[q];
+            cu[q] = add(cu[q - 1], wu[q]);
+            cv[q] = add(cv[q - 1], wv[q]);
+            cw[q] = add(cw[q - 1], ww[q]);
         }
-        const float pres_med = 0.5f * cu[point_count - 1];
+        const float pres_med = mul(0.5f, cu[point_count - 1]);
         int32_t c0, c1, c2;
         ru = median_pick(fu, cu, pres_med, &c0);
         rv = median_pick(fv, cv, pres_med, &c1);
@@ -449,11 +441,9 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     out.pwu[index] = S.pwu[index];
     out.pwv[index] = S.pwv[index];
     if (finest) {
-        const float inv_f = 2.f * tanf(0.5f * p.fovh) / float(p.cols);
         if (depth_old > 0) {
-            dx[index] = rw;
-            dy[index] = depth_old * ru * inv_f + rw * o.xx[index] / depth_old;
-            dz[index] = depth_old * rv * inv_f + rw * o.yy[index] / depth_old;
+            motion_field(depth_old, ru, rv, rw, o.xx[index], o.yy[index], inv_focal(p.fovh, p.cols), dx[index],
+                         dy[index], dz[index]);
         } else {
             dx[index] = 0.f;
             dy[index] = 0.f;

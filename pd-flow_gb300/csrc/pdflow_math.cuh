@@ -3,87 +3,132 @@
 // Each function restates one per-pixel step of the reference
 // (pdflow_cudalib.cu) as a pure function of the values it reads, so that the
 // kernels are free to stage those values in registers, shared memory or L2.
-// Expressions keep the reference's operand order and call the same device
-// intrinsics (fdividef, rhypotf, powf, __float2int_r*), so that nvcc forms the
-// same fused multiply-adds and the results track the reference's own CUDA
-// path, not just the mathematics.
+//
+// Bit-exactness.  The reference's kernels are plain C++ expressions that nvcc
+// contracts into fused multiply-adds as it sees fit; where an expression adds
+// two products (a*b + c*d) or a product with several uses, the contraction it
+// picks decides the last bit, and over hundreds of non-smooth iterations the
+// last bit decides branch outcomes.  Every operation below is therefore
+// written with an explicit rounding intrinsic (__fmaf_rn, __fmul_rn,
+// __fadd_rn, ...; nvcc never re-associates or fuses these), in the form the
+// reference's own build (nvcc 13.0, sm_103a) produces for that expression.
+// Those forms were identified by replaying the reference's per-level and
+// per-iteration state; with them the solver reproduces the reference's output
+// bit for bit (tests/test_gpu_parity.py).  Where the reference calls a device
+// intrinsic (fdividef, rhypotf, powf, tanf, __float2int_r*) it is called
+// here too.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
 
 namespace pdflow {
 
+__device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float qt(float a, float b) { return __fdiv_rn(a, b); }
+
 // 5x5 binomial mask (1,4,6,4,1)x(1,4,6,4,1)/256 (scene_flow_impair.cpp:55-58),
-// indexed [2+k + 5*(2+l)] for row offset k and column offset l.
+// for row offset k and column offset l in [-2, 2].
 __device__ __forceinline__ float gmask(int k, int l)
 {
     const int a = (k == 0) ? 6 : ((k == 1 || k == -1) ? 4 : 1);
     const int b = (l == 0) ? 6 : ((l == 1 || l == -1) ? 4 : 1);
-    return float(a * b) / 256.f;
+    return float(a * b) / 256.f;   // exact
 }
 
 // Depth decode of the reference's loader: uint16 * (float)(1/5000)
-// (scene_flow_impair.cpp:242, :269 via OpenCV convertTo). Exact product, rounded once.
-__device__ __forceinline__ float decode_depth(unsigned short d)
+// (scene_flow_impair.cpp:242, :269 via OpenCV convertTo). One rounding.
+__device__ __forceinline__ float decode_depth(unsigned short d) { return __fmul_rn(float(d), 0.0002f); }
+
+// Focal factor 2*tan(fovh/2)/cols of computePyramidLevel (pdflow_cudalib.cu:428)
+// and computeMotionField (:1152).
+__device__ __forceinline__ float inv_focal(float fovh, unsigned cols)
 {
-    return __fmul_rn(float(d), 0.0002f);
+    return qt(mul(2.f, tanf(mul(0.5f, fovh))), float(cols));
+}
+
+// Back-projection (pdflow_cudalib.cu:428-433): ((u - (C-1)/2) * z) * inv_f.
+__device__ __forceinline__ float backproject(unsigned u, unsigned C, float z, float inv_f)
+{
+    return mul(mul(sub(float(u), mul(0.5f, float(C - 1))), z), inv_f);
 }
 
 // Connectivity weight of computeRij (pdflow_cudalib.cu:760-778).
 __device__ __forceinline__ float rfac(float a, float b)
 {
-    return (fabsf(a) + fabsf(b) > 0.f) ? 2.f * rhypotf(a, b) : 1.f;
+    return (add(fabsf(a), fabsf(b)) > 0.f) ? mul(2.f, rhypotf(a, b)) : 1.f;
 }
 
-// interpolatePixel (pdflow_cudalib.cu:654-682) over a column-major plane.
+// Interpolation weights / taps of interpolatePixel (pdflow_cudalib.cu:654-682).
+struct Bilin {
+    float iu, iv;
+    unsigned su, fu, sv, fv;
+};
+
+__device__ __forceinline__ Bilin bilin(unsigned R, unsigned C, float ind_u, float ind_v)
+{
+    if (ind_u < 0.f) ind_u = 0.f;
+    else if (ind_u > sub(float(C), 1.f)) ind_u = sub(float(C), 1.f);
+    if (ind_v < 0.f) ind_v = 0.f;
+    else if (ind_v > sub(float(R), 1.f)) ind_v = sub(float(R), 1.f);
+    Bilin b;
+    b.iu = ind_u;
+    b.iv = ind_v;
+    b.su = __float2int_ru(ind_u);
+    b.fu = __float2int_rd(ind_u);
+    b.sv = __float2int_ru(ind_v);
+    b.fv = __float2int_rd(ind_v);
+    return b;
+}
+
+// Blend of the four taps (identical for interpolatePixel and the non-hole
+// branch of interpolatePixelDepth; lrintf and lroundf coincide on the
+// integral positions they are applied to).
+__device__ __forceinline__ float bilin_blend(const float* __restrict__ mat, unsigned R, const Bilin& b)
+{
+    if ((b.su == b.fu) && (b.sv == b.fv)) return mat[lrintf(fm(float(R), b.iu, b.iv))];
+    if (b.su == b.fu) {
+        const long cu = lrintf(b.iu);
+        return fm(sub(float(b.sv), b.iv), mat[b.fv + R * cu], mul(sub(b.iv, float(b.fv)), mat[b.sv + R * cu]));
+    }
+    if (b.sv == b.fv) {
+        const long cv = lrintf(b.iv);
+        return fm(sub(float(b.su), b.iu), mat[cv + R * b.fu], mul(sub(b.iu, float(b.fu)), mat[cv + R * b.su]));
+    }
+    const float A = sub(float(b.su), b.iu), B = sub(b.iu, float(b.fu));
+    const float val_sup_v = fm(A, mat[b.sv + R * b.fu], mul(B, mat[b.sv + R * b.su]));
+    const float val_inf_v = fm(A, mat[b.fv + R * b.fu], mul(B, mat[b.fv + R * b.su]));
+    return fm(sub(b.iv, float(b.fv)), val_sup_v, mul(sub(float(b.sv), b.iv), val_inf_v));
+}
+
 __device__ __forceinline__ float interp(const float* __restrict__ mat, unsigned R, unsigned C, float ind_u,
                                         float ind_v)
 {
-    if (ind_u < 0.f) ind_u = 0.f;
-    else if (ind_u > C - 1.f) ind_u = C - 1.f;
-    if (ind_v < 0.f) ind_v = 0.f;
-    else if (ind_v > R - 1.f) ind_v = R - 1.f;
-    const unsigned sup_u = __float2int_ru(ind_u);
-    const unsigned inf_u = __float2int_rd(ind_u);
-    const unsigned sup_v = __float2int_ru(ind_v);
-    const unsigned inf_v = __float2int_rd(ind_v);
-    if ((sup_u == inf_u) && (sup_v == inf_v)) return mat[lrintf(ind_v + R * ind_u)];
-    if (sup_u == inf_u)
-        return (sup_v - ind_v) * mat[inf_v + R * lrintf(ind_u)] + (ind_v - inf_v) * mat[sup_v + R * lrintf(ind_u)];
-    if (sup_v == inf_v)
-        return (sup_u - ind_u) * mat[lrintf(ind_v) + R * inf_u] + (ind_u - inf_u) * mat[lrintf(ind_v) + R * sup_u];
-    const float val_sup_v = (sup_u - ind_u) * mat[sup_v + R * inf_u] + (ind_u - inf_u) * mat[sup_v + R * sup_u];
-    const float val_inf_v = (sup_u - ind_u) * mat[inf_v + R * inf_u] + (ind_u - inf_u) * mat[inf_v + R * sup_u];
-    return (sup_v - ind_v) * val_inf_v + (ind_v - inf_v) * val_sup_v;
+    return bilin_blend(mat, R, bilin(R, C, ind_u, ind_v));
 }
 
-// interpolatePixelDepth (pdflow_cudalib.cu:684-721): nearest sample when any
-// of the four taps is a hole.
+// interpolatePixelDepth (pdflow_cudalib.cu:684-721): nearest sample
+// (round-half-even) when any of the four taps is a hole.
 __device__ __forceinline__ float interp_depth(const float* __restrict__ mat, unsigned R, unsigned C, float ind_u,
                                               float ind_v)
 {
-    if (ind_u < 0.f) ind_u = 0.f;
-    else if (ind_u > C - 1.f) ind_u = C - 1.f;
-    if (ind_v < 0.f) ind_v = 0.f;
-    else if (ind_v > R - 1.f) ind_v = R - 1.f;
-    const unsigned sup_u = __float2int_ru(ind_u);
-    const unsigned inf_u = __float2int_rd(ind_u);
-    const unsigned sup_v = __float2int_ru(ind_v);
-    const unsigned inf_v = __float2int_rd(ind_v);
-    if ((mat[sup_v + R * sup_u] == 0.f) || (mat[sup_v + R * inf_u] == 0.f) || (mat[inf_v + R * sup_u] == 0.f) ||
-        (mat[inf_v + R * inf_u] == 0.f)) {
-        const unsigned rind_u = __float2int_rn(ind_u);
-        const unsigned rind_v = __float2int_rn(ind_v);
+    const Bilin b = bilin(R, C, ind_u, ind_v);
+    if ((mat[b.sv + R * b.su] == 0.f) || (mat[b.sv + R * b.fu] == 0.f) || (mat[b.fv + R * b.su] == 0.f) ||
+        (mat[b.fv + R * b.fu] == 0.f)) {
+        const unsigned rind_u = __float2int_rn(b.iu);
+        const unsigned rind_v = __float2int_rn(b.iv);
         return mat[rind_v + R * rind_u];
     }
-    if ((sup_u == inf_u) && (sup_v == inf_v)) return mat[lrintf(ind_v + R * ind_u)];
-    if (sup_u == inf_u)
-        return (sup_v - ind_v) * mat[inf_v + R * lroundf(ind_u)] + (ind_v - inf_v) * mat[sup_v + R * lroundf(ind_u)];
-    if (sup_v == inf_v)
-        return (sup_u - ind_u) * mat[lroundf(ind_v) + R * inf_u] + (ind_u - inf_u) * mat[lroundf(ind_v) + R * sup_u];
-    const float val_sup_v = (sup_u - ind_u) * mat[sup_v + R * inf_u] + (ind_u - inf_u) * mat[sup_v + R * sup_u];
-    const float val_inf_v = (sup_u - ind_u) * mat[inf_v + R * inf_u] + (ind_u - inf_u) * mat[inf_v + R * sup_u];
-    return (sup_v - ind_v) * val_inf_v + (ind_v - inf_v) * val_sup_v;
+    return bilin_blend(mat, R, b);
+}
+
+// Gradient of computeImGradients (pdflow_cudalib.cu:593-599): weighted
+// central difference (w*(f1-f0) + wm*(f0-fm)) / (w + wm).
+__device__ __forceinline__ float wgrad(float w, float wm, float f1, float f0, float fm_)
+{
+    return qt(fm(w, sub(f1, f0), mul(wm, sub(f0, fm_))), add(w, wm));
 }
 
 // Step sizes of computeMu + computeStepSizes (pdflow_cudalib.cu:781-808).
@@ -91,22 +136,28 @@ struct Steps {
     float mu, spd, spuvx, spuvy, spwx, spwy, tu, tv, tw;
 };
 
+__device__ __forceinline__ float data_weight(float mu_p, float ddu, float ddv, float ddt)
+{
+    const float s = fm(ddt, ddt, fm(ddu, ddu, mul(ddv, ddv)));
+    return fdividef(mu_p, fm(1000.f, s, 1.f));
+}
+
 __device__ __forceinline__ Steps mu_and_steps(float mu_p, float li, float ld, float ddu, float ddv, float ddt, float ri,
                                               float rj, float ri_um1, float rj_vm1, bool has_um1, bool has_vm1)
 {
     Steps s;
-    s.mu = fdividef(mu_p, 1.f + 1000.f * (ddu * ddu + ddv * ddv + ddt * ddt));
-    s.spd = fdividef(1.f, s.mu * (1.f + fabsf(ddu) + fabsf(ddv)) + 1e-10f);
-    s.spuvx = fdividef(0.5f, li * ri + 1e-10f);
-    s.spuvy = fdividef(0.5f, li * rj + 1e-10f);
-    s.spwx = fdividef(0.5f, ri * ld + 1e-10f);
-    s.spwy = fdividef(0.5f, rj * ld + 1e-10f);
-    float acu_r = ri + rj;
-    if (has_um1) acu_r += ri_um1;
-    if (has_vm1) acu_r += rj_vm1;
-    s.tu = fdividef(1.f, s.mu * fabsf(ddu) + li * acu_r + 1e-10f);
-    s.tv = fdividef(1.f, s.mu * fabsf(ddv) + li * acu_r + 1e-10f);
-    s.tw = fdividef(1.f, s.mu + ld * acu_r + 1e-10f);
+    s.mu = data_weight(mu_p, ddu, ddv, ddt);
+    s.spd = fdividef(1.f, fm(s.mu, add(add(1.f, fabsf(ddu)), fabsf(ddv)), 1e-10f));
+    s.spuvx = fdividef(0.5f, fm(li, ri, 1e-10f));
+    s.spuvy = fdividef(0.5f, fm(li, rj, 1e-10f));
+    s.spwx = fdividef(0.5f, fm(ri, ld, 1e-10f));
+    s.spwy = fdividef(0.5f, fm(rj, ld, 1e-10f));
+    float acu_r = add(ri, rj);
+    if (has_um1) acu_r = add(acu_r, ri_um1);
+    if (has_vm1) acu_r = add(acu_r, rj_vm1);
+    s.tu = fdividef(1.f, add(fm(li, acu_r, mul(s.mu, fabsf(ddu))), 1e-10f));
+    s.tv = fdividef(1.f, add(fm(li, acu_r, mul(s.mu, fabsf(ddv))), 1e-10f));
+    s.tw = fdividef(1.f, add(fm(ld, acu_r, s.mu), 1e-10f));
     return s;
 }
 
@@ -118,6 +169,20 @@ struct Duals {
     float pd, puu, puv, pvu, pvv, pwu, pwv;
 };
 
+__device__ __forceinline__ float fwd_diff(float r, float a1, float p1, float a0, float p0)
+{
+    return mul(r, sub(add(a1, p1), add(a0, p0)));
+}
+
+__device__ __forceinline__ void project_disc(float& a, float& b)
+{
+    const float m = rhypotf(a, b);
+    if (m < 1.f) {
+        a = mul(a, m);
+        b = mul(b, m);
+    }
+}
+
 __device__ __forceinline__ void dual_update(Duals& p, float spd, float spuvx, float spuvy, float spwx, float spwy,
                                             float mu, float ddt, float ddu, float ddv, float li, float ld, float ri,
                                             float rj, float dua, float dva, float dwa, float dup, float dvp,
@@ -125,41 +190,26 @@ __device__ __forceinline__ void dual_update(Duals& p, float spd, float spuvx, fl
                                             float dua_v1, float dva_v1, float dwa_v1, float dup_v1, float dvp_v1,
                                             bool last_u, bool last_v)
 {
-    float gu1, gv1, gw1, gu2, gv2, gw2;
-    if (last_u) {
-        gu1 = 0.f; gv1 = 0.f; gw1 = 0.f;
-    } else {
-        gu1 = ri * ((dua_u1 + dup_u1) - (dua + dup));
-        gv1 = ri * ((dva_u1 + dvp_u1) - (dva + dvp));
-        gw1 = ri * (dwa_u1 - dwa);
-    }
-    if (last_v) {
-        gu2 = 0.f; gv2 = 0.f; gw2 = 0.f;
-    } else {
-        gu2 = rj * ((dua_v1 + dup_v1) - (dua + dup));
-        gv2 = rj * ((dva_v1 + dvp_v1) - (dva + dvp));
-        gw2 = rj * (dwa_v1 - dwa);
-    }
-    float pd = p.pd, puu = p.puu, puv = p.puv, pvu = p.pvu, pvv = p.pvv, pwu = p.pwu, pwv = p.pwv;
-    pd += spd * mu * (-dwa + ddt + ddu * dua + ddv * dva);
-    puu += spuvx * li * gu1;
-    puv += spuvy * li * gu2;
-    pvu += spuvx * li * gv1;
-    pvv += spuvy * li * gv2;
-    pwu += spwx * ld * gw1;
-    pwv += spwy * ld * gw2;
-    float m = fabsf(pd);
-    if (m > 1.f) p.pd = (pd > 1.f) ? 1.f : -1.f;
-    else p.pd = pd;
-    m = rhypotf(puu, puv);
-    if (m < 1.f) { p.puu = puu * m; p.puv = puv * m; }
-    else { p.puu = puu; p.puv = puv; }
-    m = rhypotf(pvu, pvv);
-    if (m < 1.f) { p.pvu = pvu * m; p.pvv = pvv * m; }
-    else { p.pvu = pvu; p.pvv = pvv; }
-    m = rhypotf(pwu, pwv);
-    if (m < 1.f) { p.pwu = pwu * m; p.pwv = pwv * m; }
-    else { p.pwu = pwu; p.pwv = pwv; }
+    const float gu1 = last_u ? 0.f : fwd_diff(ri, dua_u1, dup_u1, dua, dup);
+    const float gv1 = last_u ? 0.f : fwd_diff(ri, dva_u1, dvp_u1, dva, dvp);
+    const float gw1 = last_u ? 0.f : mul(ri, sub(dwa_u1, dwa));
+    const float gu2 = last_v ? 0.f : fwd_diff(rj, dua_v1, dup_v1, dua, dup);
+    const float gv2 = last_v ? 0.f : fwd_diff(rj, dva_v1, dvp_v1, dva, dvp);
+    const float gw2 = last_v ? 0.f : mul(rj, sub(dwa_v1, dwa));
+    const float X = fm(ddv, dva, fm(ddu, dua, add(-dwa, ddt)));
+    float pd = fm(mul(spd, mu), X, p.pd);
+    const float sx = mul(spuvx, li), sy = mul(spuvy, li), wx = mul(spwx, ld), wy = mul(spwy, ld);
+    float puu = fm(sx, gu1, p.puu), puv = fm(sy, gu2, p.puv);
+    float pvu = fm(sx, gv1, p.pvu), pvv = fm(sy, gv2, p.pvv);
+    float pwu = fm(wx, gw1, p.pwu), pwv = fm(wy, gw2, p.pwv);
+    if (fabsf(pd) > 1.f) pd = (pd > 1.f) ? 1.f : -1.f;
+    project_disc(puu, puv);
+    project_disc(pvu, pvv);
+    project_disc(pwu, pwv);
+    p.pd = pd;
+    p.puu = puu; p.puv = puv;
+    p.pvu = pvu; p.pvv = pvv;
+    p.pwu = pwu; p.pwv = pwv;
 }
 
 // Divergence term of computeDivergence (pdflow_cudalib.cu:935-980) for one
@@ -169,12 +219,12 @@ __device__ __forceinline__ float divergence(float ri, float ri_um1, float rj, fl
                                             bool last_v)
 {
     float d;
-    if (first_u) d = ri * pu;
-    else if (last_u) d = -ri_um1 * pu_um1;
-    else d = ri * pu - ri_um1 * pu_um1;
-    if (first_v) d += rj * pv;
-    else if (last_v) d += -rj_vm1 * pv_vm1;
-    else d += rj * pv - rj_vm1 * pv_vm1;
+    if (first_u) d = mul(ri, pu);
+    else if (last_u) d = mul(-ri_um1, pu_um1);
+    else d = fm(ri, pu, -mul(ri_um1, pu_um1));
+    if (first_v) d = fm(rj, pv, d);
+    else if (last_v) d = fm(-rj_vm1, pv_vm1, d);
+    else d = add(d, fm(rj, pv, -mul(rj_vm1, pv_vm1)));
     return d;
 }
 
@@ -187,25 +237,26 @@ __device__ __forceinline__ void primal_update(float& du, float& dv, float& dw, f
                                               float dcu, float dcv)
 {
     const float du_old = du, dv_old = dv, dw_old = dw;
-    du += -tu * (mu * ddu * pd - li * divu);
-    dv += -tv * (mu * ddv * pd - li * divv);
-    dw += -tw * (-mu * pd - ld * divw);
-    const float optflow = dct + dcu * du + dcv * dv;
-    const float of_threshold = tu * dcu * dcu + tv * dcv * dcv;
+    du = fm(-tu, fm(mul(mu, ddu), pd, -mul(li, divu)), du);
+    dv = fm(-tv, fm(mul(mu, ddv), pd, -mul(li, divv)), dv);
+    dw = add(dw, mul(-tw, fm(-mu, pd, -mul(ld, divw))));
+    const float optflow = fm(dcv, dv, fm(dcu, du, dct));
+    const float a1 = mul(tu, dcu), b1 = mul(tv, dcv);
+    const float of_threshold = fm(a1, dcu, mul(b1, dcv));
     if (optflow < -of_threshold) {
-        du += tu * dcu;
-        dv += tv * dcv;
+        du = add(du, a1);
+        dv = add(dv, b1);
     } else if (optflow > of_threshold) {
-        du -= tu * dcu;
-        dv -= tv * dcv;
+        du = sub(du, a1);
+        dv = sub(dv, b1);
     } else {
-        const float den = tu * dcu * dcu + tv * dcv * dcv + 1e-10f;
-        du -= tu * dcu * optflow / den;
-        dv -= tv * dcv * optflow / den;
+        const float den = add(fm(a1, dcu, mul(b1, dcv)), 1e-10f);
+        du = sub(du, qt(mul(a1, optflow), den));
+        dv = sub(dv, qt(mul(b1, optflow), den));
     }
-    dua = 2.f * du - du_old;
-    dva = 2.f * dv - dv_old;
-    dwa = 2.f * dw - dw_old;
+    dua = fm(2.f, du, -du_old);
+    dva = fm(2.f, dv, -dv_old);
+    dwa = fm(2.f, dw, -dw_old);
 }
 
 // saturateVariables (pdflow_cudalib.cu:1018-1038).
@@ -217,8 +268,31 @@ __device__ __forceinline__ void saturate(float& du, float& dv, float& dw, float 
     if (dv > 1.f) dv = 1.f;
     else if (dv < -1.f) dv = -1.f;
     if (depth_old == 0.f) dw = 0.f;
-    du = du + du_prev;
-    dv = dv + dv_prev;
+    du = add(du, du_prev);
+    dv = add(dv, dv_prev);
+}
+
+// Weight of a neighbour in filterSolution (pdflow_cudalib.cu:1075):
+// 1 / (1 + 5 (z0 - z)^2 + 10 ddt^2).
+__device__ __forceinline__ float median_weight(float z0, float z, float ddt)
+{
+    return qt(1.f, fm(10.f, powf(ddt, 2.f), fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
+}
+
+// Linear interpolation between the samples bracketing the weighted median
+// (pdflow_cudalib.cu:1109).
+__device__ __forceinline__ float median_lerp(float cum_r, float cum_l, float med, float f_l, float f_r)
+{
+    return qt(fm(sub(cum_r, med), f_l, mul(sub(med, cum_l), f_r)), sub(cum_r, cum_l));
+}
+
+// computeMotionField (pdflow_cudalib.cu:1155-1160) at a pixel with depth z > 0.
+__device__ __forceinline__ void motion_field(float z, float du, float dv_, float dw, float xx, float yy, float inv_f,
+                                             float& dx, float& dy, float& dz)
+{
+    dx = dw;
+    dy = fm(mul(z, du), inv_f, qt(mul(dw, xx), z));
+    dz = fm(mul(z, dv_), inv_f, qt(mul(dw, yy), z));
 }
 
 }  // namespace pdflow
