@@ -24,6 +24,12 @@ typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const flo
  * in CSF_cuda, pdflow_cudalib.h:71-122).  The final flow equals pdflow_solve's. */
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
+/* Selects how pdflow_solve runs a level's iterations: 1 (default) = one
+ * launch per level (slab-persistent kernel), 0 = two kernels per iteration
+ * (the reference's launch structure with gradient+dual and divergence+primal
+ * fused).  Both give the same bits. */
+int pdflow_set_iteration_form(pdflow_solver* s, int form);
+
 /* The 3x3 weighted median of filterSolution (pdflow_cudalib.cu:1040-1148) on
  * caller planes (device pointers, R*C floats, column-major).  `sel` (device,
  * 3*R*C int32, may be NULL) receives, per component, the bracketing index the

@@ -113,6 +113,21 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
     return PDFLOW_OK;
 }
 
+int pdflow_set_iteration_form(pdflow_solver* s, int form)
+{
+    if (!s || (form != 0 && form != 1)) return PDFLOW_ERR_ARG;
+    if (s->iter_form != form) {
+        cudaStreamSynchronize(s->stream);
+        for (int k = 0; k < 2; ++k)
+            if (s->solve_graph[k]) {
+                cudaGraphExecDestroy(s->solve_graph[k]);
+                s->solve_graph[k] = nullptr;
+            }
+        s->iter_form = form;
+    }
+    return PDFLOW_OK;
+}
+
 int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const float* ddt, const float* du,
                         const float* dv, const float* dw, float* du_l, float* dv_l, float* dw_l, int32_t* sel,
                         void* stream)

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pdflow.h"
+#include "pdflow_iterate.cuh"
 #include "pdflow_kernels.cuh"
 
 struct pdflow_solver {
@@ -23,7 +24,12 @@ struct pdflow_solver {
     uint16_t* stage_u16 = nullptr;
     pdflow::LevelConsts L{};
     pdflow::State S{};
+    float* alt[10] = {};                 // second buffer of du_acc,dv_acc,dw_acc,pd,puu,puv,pvu,pvv,pwu,pwv
     pdflow::LevelSol sol{};
+    unsigned* flags = nullptr;           // per-CTA progress counters of the grid-form iteration
+    unsigned* status = nullptr;          // device status word (0 = ok)
+    int num_sms = 0;
+    int iter_form = 1;                   // 1 = one launch per level's iterations, 0 = two kernels per iteration
     float* dx = nullptr;
     float* dy = nullptr;
     float* dz = nullptr;
@@ -35,5 +41,6 @@ namespace pdflow {
 void carve_solver(pdflow_solver* s, char* base, size_t* used);
 int enqueue_pyramid(pdflow_solver* s, cudaStream_t st);
 int enqueue_solve(pdflow_solver* s, cudaStream_t st);
+int check_status(pdflow_solver* s);
 LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image);
 }  // namespace pdflow

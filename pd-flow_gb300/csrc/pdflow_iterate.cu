@@ -1,0 +1,347 @@
+// The primal-dual iterations of one pyramid level in a single launch.
+//
+// Each CTA owns a slab of columns [u0, u1) of the level (column-major
+// planes: a column is R contiguous floats, so a slab is one contiguous range).
+// Per iteration it
+//   1. computes the dual step (gradient + updateDualVariables) on its columns
+//      and, redundantly, on the column u0-1 of its left neighbour, into shared
+//      memory (the primal's backward divergence needs the new duals one
+//      column to the left);
+//   2. computes the primal step (divergence + updatePrimalVariables) on its
+//      own columns.
+// The over-relaxed primal (du_acc, dv_acc, dw_acc) and the duals are double
+// buffered (iteration t reads buffer t&1 and writes buffer (t+1)&1), so the
+// only synchronisation is one wait per iteration for the two neighbouring
+// slabs to have finished the previous iteration.  The wait is
+//   - nothing (one CTA owns the level),
+//   - the hardware cluster barrier (the level fits one thread-block cluster), or
+//   - per-CTA progress counters in global memory, spun on with a bounded
+//     count (a cooperative launch keeps every CTA resident).  A wait that
+//     runs out sets an error code in the status word and the kernel returns.
+// Data written by another CTA is read with ld.global.cg (L2), never through a
+// possibly stale L1 line.  Per-pixel arithmetic is pdflow_math.cuh, identical
+// to the stage kernels, so the results are bit-for-bit the same.
+#include <cooperative_groups.h>
+
+#include "pdflow_iterate.cuh"
+#include "pdflow_math.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pdflow {
+
+namespace {
+
+constexpr unsigned kIterThreads = 1024;
+constexpr unsigned long long kSpinLimit = 1ull << 24;   // ~seconds of polling, then give up
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 waits until both neighbouring slabs have completed `need`
+// iterations.  Returns false (after recording the failure) on timeout.
+__device__ bool wait_neighbours(const IterArgs& a, unsigned need)
+{
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned b = blockIdx.x;
+        unsigned long long spins = 0;
+        if (b > 0)
+            while (ld_acquire(a.flags + b - 1) < need) {
+                if (++spins > kSpinLimit || ld_acquire(a.status) != 0) { ok = 0; break; }
+            }
+        if (ok && b + 1 < gridDim.x)
+            while (ld_acquire(a.flags + b + 1) < need) {
+                if (++spins > kSpinLimit || ld_acquire(a.status) != 0) { ok = 0; break; }
+            }
+        if (!ok) atomicCAS(a.status, 0u, kStatusTimeout);
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Shared-memory layout of a CTA (slab of W = u1-u0 columns, halo column h0 = u0-1):
+//   13 state planes over the slab:  du dv dw | du_acc dv_acc dw_acc | pd puu puv pvu pvv pwu pwv
+//    7 planes of new duals over [h0, u1)
+enum { SDU, SDV, SDW, SUA, SVA, SWA, SPD, SPUU, SPUV, SPVU, SPVV, SPWU, SPWV, SNST };
+
+template <int kMode>
+__global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
+{
+    extern __shared__ float sm[];
+    const unsigned R = a.g.R, C = a.g.C;
+    const unsigned nb = gridDim.x, b = blockIdx.x;
+    const unsigned u0 = (unsigned)((unsigned long long)b * C / nb);
+    const unsigned u1 = (unsigned)((unsigned long long)(b + 1) * C / nb);
+    const unsigned h0 = (u0 > 0) ? u0 - 1 : 0;
+    const unsigned nown = (u1 - u0) * R;          // own pixels
+    const unsigned nsp = (u1 - h0) * R;           // pixels with a dual in this CTA
+    const unsigned off = (u0 - h0) * R;           // index of the first own pixel in the dual planes
+    const unsigned ps = a.smem_state_plane;       // floats per state plane (>= nown)
+    const unsigned pq = a.smem_plane;             // floats per dual plane (>= nsp)
+    float* st = sm;                               // SNST planes, own pixels at [0, nown)
+    float* np = sm + SNST * ps;                   // 7 planes of new duals, [0, nsp)
+    const LevelConsts& L = a.L;
+    const float li = a.p.lambda_i, ld = a.p.lambda_d;
+    const bool has_left = (u0 > 0), has_right = (u1 < C);
+
+    // initial state of the level (written by the set-up kernel into buffer 0)
+    for (unsigned j = threadIdx.x; j < nown; j += blockDim.x) {
+        const unsigned i = u0 * R + j;
+        st[SDU * ps + j] = a.du[i];
+        st[SDV * ps + j] = a.dv[i];
+        st[SDW * ps + j] = a.dw[i];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) st[(SUA + k) * ps + j] = __ldcg(a.acc[0][k] + i);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) st[(SPD + k) * ps + j] = __ldcg(a.p_[0][k] + i);
+    }
+    __syncthreads();
+
+    for (unsigned t = 0; t < a.iters; ++t) {
+        const int cur = t & 1, nxt = cur ^ 1;
+        if (t > 0) {
+            if (kMode == kIterGrid) {
+                if (!wait_neighbours(a, t)) return;
+            } else if (kMode == kIterCluster) {
+                cg::this_cluster().sync();
+            }
+        }
+        // ---- dual step over [h0, u1) ----
+        for (unsigned j = threadIdx.x; j < nsp; j += blockDim.x) {
+            const unsigned v = j % R, u = h0 + j / R, i = v + u * R;
+            const bool own = (u >= u0);
+            const unsigned jo = j - off;          // own-slab index (valid when own)
+            const bool lu = (u == C - 1), lv = (v == R - 1);
+            float dua, dva, dwa, dua_u, dva_u, dwa_u, dua_v, dva_v, dwa_v;
+            Duals d;
+            if (own) {
+                dua = st[SUA * ps + jo]; dva = st[SVA * ps + jo]; dwa = st[SWA * ps + jo];
+                d = Duals{st[SPD * ps + jo], st[SPUU * ps + jo], st[SPUV * ps + jo], st[SPVU * ps + jo],
+                          st[SPVV * ps + jo], st[SPWU * ps + jo], st[SPWV * ps + jo]};
+                const unsigned jv = lv ? jo : jo + 1;
+                dua_v = st[SUA * ps + jv]; dva_v = st[SVA * ps + jv]; dwa_v = st[SWA * ps + jv];
+            } else {
+                // halo column u0-1: the left neighbour's state of this iteration
+                dua = __ldcg(a.acc[cur][0] + i); dva = __ldcg(a.acc[cur][1] + i); dwa = __ldcg(a.acc[cur][2] + i);
+                d = Duals{__ldcg(a.p_[cur][0] + i), __ldcg(a.p_[cur][1] + i), __ldcg(a.p_[cur][2] + i),
+                          __ldcg(a.p_[cur][3] + i), __ldcg(a.p_[cur][4] + i), __ldcg(a.p_[cur][5] + i),
+                          __ldcg(a.p_[cur][6] + i)};
+                const unsigned iv = lv ? i : i + 1;
+                dua_v = __ldcg(a.acc[cur][0] + iv); dva_v = __ldcg(a.acc[cur][1] + iv);
+                dwa_v = __ldcg(a.acc[cur][2] + iv);
+            }
+            if (lu) {
+                dua_u = dua; dva_u = dva; dwa_u = dwa;
+            } else if (u + 1 < u1) {
+                const unsigned ju = (u + 1 - u0) * R + v;   // own column to the right
+                dua_u = st[SUA * ps + ju]; dva_u = st[SVA * ps + ju]; dwa_u = st[SWA * ps + ju];
+            } else {
+                // column u1: the right neighbour's first column
+                dua_u = __ldcg(a.acc[cur][0] + i + R); dva_u = __ldcg(a.acc[cur][1] + i + R);
+                dwa_u = __ldcg(a.acc[cur][2] + i + R);
+            }
+            const unsigned iu = lu ? i : i + R, iv = lv ? i : i + 1;
+            dual_update(d, __ldg(L.spd + i), __ldg(L.spuvx + i), __ldg(L.spuvy + i), __ldg(L.spwx + i),
+                        __ldg(L.spwy + i), __ldg(L.mu + i), __ldg(L.ddt + i), __ldg(L.ddu + i), __ldg(L.ddv + i), li,
+                        ld, __ldg(L.ri + i), __ldg(L.rj + i), dua, dva, dwa, __ldg(L.du_prev + i),
+                        __ldg(L.dv_prev + i), dua_u, dva_u, dwa_u, __ldg(L.du_prev + iu), __ldg(L.dv_prev + iu), dua_v,
+                        dva_v, dwa_v, __ldg(L.du_prev + iv), __ldg(L.dv_prev + iv), lu, lv);
+            np[0 * pq + j] = d.pd;
+            np[1 * pq + j] = d.puu;
+            np[2 * pq + j] = d.puv;
+            np[3 * pq + j] = d.pvu;
+            np[4 * pq + j] = d.pvv;
+            np[5 * pq + j] = d.pwu;
+            np[6 * pq + j] = d.pwv;
+        }
+        __syncthreads();
+        // ---- primal step over [u0, u1) ----
+        const bool last = (t + 1 == a.iters);
+        for (unsigned j = threadIdx.x; j < nown; j += blockDim.x) {
+            const unsigned v = j % R, u = u0 + j / R, i = v + u * R;
+            const unsigned jl = off + j;                   // index in the dual planes
+            const bool fu = (u == 0), lu = (u == C - 1), fv = (v == 0), lv = (v == R - 1);
+            const unsigned jum = fu ? jl : jl - R, jvm = fv ? jl : jl - 1;
+            const float ri = __ldg(L.ri + i), rj = __ldg(L.rj + i);
+            const float ri_m = fu ? ri : __ldg(L.ri + i - R), rj_m = fv ? rj : __ldg(L.rj + i - 1);
+            float pn[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) pn[k] = np[k * pq + jl];
+            const float divu = divergence(ri, ri_m, rj, rj_m, pn[1], np[1 * pq + jum], pn[2], np[2 * pq + jvm], fu, lu,
+                                          fv, lv);
+            const float divv = divergence(ri, ri_m, rj, rj_m, pn[3], np[3 * pq + jum], pn[4], np[4 * pq + jvm], fu, lu,
+                                          fv, lv);
+            const float divw = divergence(ri, ri_m, rj, rj_m, pn[5], np[5 * pq + jum], pn[6], np[6 * pq + jvm], fu, lu,
+                                          fv, lv);
+            float du = st[SDU * ps + j], dv = st[SDV * ps + j], dw = st[SDW * ps + j], nua, nva, nwa;
+            primal_update(du, dv, dw, nua, nva, nwa, __ldg(L.tu + i), __ldg(L.tv + i), __ldg(L.tw + i),
+                          __ldg(L.mu + i), __ldg(L.ddu + i), __ldg(L.ddv + i), pn[0], li, ld, divu, divv, divw,
+                          __ldg(L.dct + i), __ldg(L.dcu + i), __ldg(L.dcv + i));
+            if (last) saturate(du, dv, dw, __ldg(L.du_prev + i), __ldg(L.dv_prev + i), __ldg(a.depth_old + i));
+            st[SDU * ps + j] = du;
+            st[SDV * ps + j] = dv;
+            st[SDW * ps + j] = dw;
+            st[SUA * ps + j] = nua;
+            st[SVA * ps + j] = nva;
+            st[SWA * ps + j] = nwa;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) st[(SPD + k) * ps + j] = pn[k];
+            if (!last) {
+                // publish the columns the neighbours read in the next iteration
+                if (has_left && u == u0) {
+                    __stcg(a.acc[nxt][0] + i, nua);
+                    __stcg(a.acc[nxt][1] + i, nva);
+                    __stcg(a.acc[nxt][2] + i, nwa);
+                }
+                if (has_right && u == u1 - 1) {
+                    __stcg(a.acc[nxt][0] + i, nua);
+                    __stcg(a.acc[nxt][1] + i, nva);
+                    __stcg(a.acc[nxt][2] + i, nwa);
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) __stcg(a.p_[nxt][k] + i, pn[k]);
+                }
+            }
+        }
+        __syncthreads();
+        if (kMode == kIterGrid && !last) {
+            if (threadIdx.x == 0) {
+                __threadfence();
+                st_release(a.flags + b, t + 1);
+            }
+        }
+    }
+    // Final state for the weighted median: saturated (du, dv, dw) and the duals.
+    // The duals go to buffer (iters & 1): the neighbours may still be reading
+    // buffer ((iters - 1) & 1) in their last iteration, and nobody reads the
+    // other one any more.
+    const int fb = a.iters & 1;
+    for (unsigned j = threadIdx.x; j < nown; j += blockDim.x) {
+        const unsigned i = u0 * R + j;
+        a.du[i] = st[SDU * ps + j];
+        a.dv[i] = st[SDV * ps + j];
+        a.dw[i] = st[SDW * ps + j];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) a.p_[fb][k][i] = st[(SPD + k) * ps + j];
+    }
+}
+
+unsigned g_max_cluster = 8;    // largest cluster the GPU places with this kernel's resources
+unsigned g_max_dyn_smem = 0;   // dynamic shared memory available to the iteration kernels
+
+}  // namespace
+
+unsigned iterate_smem_limit() { return g_max_dyn_smem; }
+
+IterPlan plan_iterate(LevelGeom g, int num_sms)
+{
+    IterPlan pl;
+    if (g.N <= 1200 || g.C < 8) {
+        pl.mode = kIterSingle;
+        pl.ctas = 1;
+    } else if (g.N <= 19200) {
+        pl.mode = kIterCluster;
+        pl.ctas = (g.C >= 160) ? g_max_cluster : 8;
+    } else {
+        pl.mode = kIterGrid;
+        unsigned s = g.C / 2;
+        if (s > (unsigned)num_sms) s = (unsigned)num_sms;
+        pl.ctas = s;
+    }
+    unsigned maxcols = 0, maxown = 0;
+    for (unsigned b = 0; b < pl.ctas; ++b) {
+        const unsigned u0 = (unsigned)((unsigned long long)b * g.C / pl.ctas);
+        const unsigned u1 = (unsigned)((unsigned long long)(b + 1) * g.C / pl.ctas);
+        const unsigned h0 = u0 > 0 ? u0 - 1 : 0;
+        if (u1 - h0 > maxcols) maxcols = u1 - h0;
+        if (u1 - u0 > maxown) maxown = u1 - u0;
+    }
+    pl.smem_plane = maxcols * g.R;
+    pl.smem_state_plane = maxown * g.R;
+    pl.smem_bytes = (size_t(13) * pl.smem_state_plane + size_t(7) * pl.smem_plane) * sizeof(float);
+    return pl;
+}
+
+template <int kMode>
+static cudaError_t allow_smem(int optin)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_iterate<kMode>);
+    if (e != cudaSuccess) return e;
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (g_max_dyn_smem == 0 || (unsigned)dyn < g_max_dyn_smem) g_max_dyn_smem = (unsigned)dyn;
+    return cudaFuncSetAttribute(k_iterate<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+}
+
+cudaError_t prepare_iterate()
+{
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_iterate<kIterCluster>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e == cudaSuccess) e = allow_smem<kIterCluster>(optin);
+    if (e == cudaSuccess) e = allow_smem<kIterGrid>(optin);
+    if (e == cudaSuccess) e = allow_smem<kIterSingle>(optin);
+    if (e != cudaSuccess) return e;
+    // Is a 16-CTA cluster of this kernel placeable (shared memory of the largest clustered level)?
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(kIterThreads);
+    cfg.dynamicSmemBytes = 100 * 1024;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = 16;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_iterate<kIterCluster>, &cfg) == cudaSuccess && nclusters > 0)
+        g_max_cluster = 16;
+    else
+        cudaGetLastError();
+    return cudaSuccess;
+}
+
+cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st)
+{
+    a.smem_plane = pl.smem_plane;
+    a.smem_state_plane = pl.smem_state_plane;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(pl.ctas);
+    cfg.blockDim = dim3(kIterThreads);
+    cfg.dynamicSmemBytes = pl.smem_bytes;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    cfg.attrs = attr;
+    cfg.numAttrs = 0;
+    if (pl.mode == kIterGrid) {
+        cudaError_t e = cudaMemsetAsync(a.flags, 0, sizeof(unsigned) * pl.ctas, st);
+        if (e != cudaSuccess) return e;
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_iterate<kIterGrid>, a);
+    }
+    if (pl.mode == kIterCluster) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = pl.ctas;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_iterate<kIterCluster>, a);
+    }
+    return cudaLaunchKernelEx(&cfg, k_iterate<kIterSingle>, a);
+}
+
+}  // namespace pdflow

@@ -1,0 +1,46 @@
+// One-launch iteration of a pyramid level (see pdflow_iterate.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pdflow_kernels.cuh"
+
+namespace pdflow {
+
+enum IterMode { kIterSingle = 0, kIterCluster = 1, kIterGrid = 2 };
+
+// Value left in the status word when a bounded wait gives up.
+constexpr unsigned kStatusTimeout = 1u;
+
+struct IterArgs {
+    LevelGeom g;
+    LevelConsts L;
+    float *du, *dv, *dw;          // primal increments (updated in place; saturated after the last iteration)
+    float* acc[2][3];             // over-relaxed primal, double buffered: [buffer][du, dv, dw]
+    float* p_[2][7];              // duals, double buffered: [buffer][pd, puu, puv, pvu, pvv, pwu, pwv]
+    Params p;
+    const float* depth_old;       // old frame depth at this level (saturation)
+    unsigned iters;
+    unsigned* flags;              // per-CTA completed-iteration counters (grid form)
+    unsigned* status;             // 0, or kStatusTimeout after a bounded wait gave up
+    unsigned smem_plane;          // floats per shared plane of new duals (set by launch_iterate)
+    unsigned smem_state_plane;    // floats per shared state plane (set by launch_iterate)
+};
+
+struct IterPlan {
+    int mode = kIterSingle;
+    unsigned ctas = 1;
+    unsigned smem_plane = 0;
+    unsigned smem_state_plane = 0;
+    size_t smem_bytes = 0;
+};
+
+// Launch shape for a level on a GPU with `num_sms` SMs.
+IterPlan plan_iterate(LevelGeom g, int num_sms);
+// Dynamic shared memory the iteration kernels may use (after prepare_iterate).
+unsigned iterate_smem_limit();
+// One-time function attributes (dynamic shared memory, cluster size).
+cudaError_t prepare_iterate();
+// Enqueues the level's iterations (and, in the grid form, the reset of the progress counters).
+cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st);
+
+}  // namespace pdflow

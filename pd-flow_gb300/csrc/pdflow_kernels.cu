@@ -358,27 +358,60 @@ __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* dep
 // ---------------------------------------------------------------------------
 // filterSolution (pdflow_cudalib.cu:1040-1148) + computeMotionField (:1150-1167)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void bubble_sort(float* f, float* w, unsigned n)
+// Weighted median of up to 9 samples, register resident.  The reference
+// bubble-sorts (value, weight) pairs (stable: bubbleSortDev swaps only on
+// a[i-1] > a[i]), accumulates the weights in sorted order and walks to the
+// first cumulative weight >= med (pdflow_cudalib.cu:1083-1132).  Here the
+// stable rank of each sample, #{j : f_j < f_i or (f_j == f_i and j < i)},
+// places it directly; every loop is unrolled over constant indices so nothing
+// spills to local memory.  Sums are taken in the same sorted order, so the
+// result and the selected index are the reference's bit for bit.
+__device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned n, float med_or_neg,
+                                         float* total, int32_t* cont_out)
 {
-    bool go_on = true;
-    while (go_on) {
-        go_on = false;
-        for (unsigned i = 1; i < n; i++)
-            if (f[i - 1] > f[i]) {
-                float t = f[i - 1]; f[i - 1] = f[i]; f[i] = t;
-                t = w[i - 1]; w[i - 1] = w[i]; w[i] = t;
-                go_on = true;
+    int rank[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        int r = 0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j)
+            if (j != i && (unsigned)j < n && (f[j] < f[i] || (f[j] == f[i] && j < i))) ++r;
+        rank[i] = r;
+    }
+    float sf[9], sw[9];
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        sf[r] = 0.f;
+        sw[r] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+            if ((unsigned)i < n && rank[i] == r) {
+                sf[r] = f[i];
+                sw[r] = w[i];
             }
     }
-}
-
-__device__ __forceinline__ float median_pick(const float* f, const float* cum, float pres_med, int32_t* cont_out)
-{
-    unsigned cont = 0;
-    while (pres_med > cum[cont]) cont++;
-    *cont_out = (int32_t)cont;
-    if (cont == 0) return f[0];
-    return median_lerp(cum[cont], cum[cont - 1], pres_med, f[cont - 1], f[cont]);
+    float cum[9];
+    cum[0] = sw[0];
+#pragma unroll
+    for (int r = 1; r < 9; ++r) cum[r] = ((unsigned)r < n) ? add(cum[r - 1], sw[r]) : cum[r - 1];
+    *total = cum[8];   // == cum[n-1]
+    const float med = (med_or_neg < 0.f) ? mul(0.5f, cum[8]) : med_or_neg;
+    int cont = 0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        if ((unsigned)r < n && med > cum[r]) ++cont;
+    *cont_out = cont;
+    if (cont == 0) return sf[0];
+    float cr = 0.f, cl = 0.f, fr = 0.f, fl = 0.f;
+#pragma unroll
+    for (int r = 1; r < 9; ++r)
+        if (r == cont) {
+            cr = cum[r];
+            cl = cum[r - 1];
+            fr = sf[r];
+            fl = sf[r - 1];
+        }
+    return median_lerp(cr, cl, med, fl, fr);
 }
 
 __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, LevelSol out, float* dx,
@@ -391,37 +424,34 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     const float depth_old = o.dep[index];
     float ru, rv, rw;
     if (depth_old > 0.f) {
-        float fu[9], fv[9], fw[9], wu[9], wv[9], ww[9];
-        unsigned point_count = 9, vi = 0;
+        float fu[9], fv[9], fw[9], wt[9];
+        unsigned n = 0;
+#pragma unroll
         for (int k = -1; k < 2; k++)
+#pragma unroll
             for (int l = -1; l < 2; l++) {
                 const int indr = (int)v + k, indc = (int)u + l;
-                if ((indr < 0) || (indr >= (int)R) || (indc < 0) || (indc >= (int)C)) {
-                    point_count--;
-                    continue;
-                }
-                const int j = (int)index + l * (int)R + k;
+                const bool in = (indr >= 0) && (indr < (int)R) && (indc >= 0) && (indc < (int)C);
+                const int j = in ? (int)index + l * (int)R + k : (int)index;
                 const float pres = median_weight(depth_old, o.dep[j], L.ddt[j]);
-                fu[vi] = S.du[j]; wu[vi] = pres;
-                fv[vi] = S.dv[j]; wv[vi] = pres;
-                fw[vi] = S.dw[j]; ww[vi] = pres;
-                vi++;
+                const float a = S.du[j], b = S.dv[j], c = S.dw[j];
+                // compact the present samples to the front, in the reference's order
+#pragma unroll
+                for (int q = 0; q < 9; ++q)
+                    if (in && (unsigned)q == n) {
+                        fu[q] = a; fv[q] = b; fw[q] = c; wt[q] = pres;
+                    }
+                if (in) ++n;
             }
-        bubble_sort(fu, wu, point_count);
-        bubble_sort(fv, wv, point_count);
-        bubble_sort(fw, ww, point_count);
-        float cu[9], cv[9], cw[9];
-        cu[0] = wu[0]; cv[0] = wv[0]; cw[0] = ww[0];
-        for (unsigned q = 1; q < point_count; q++) {
-            cu[q] = add(cu[q - 1], wu[q]);
-            cv[q] = add(cv[q - 1], wv[q]);
-            cw[q] = add(cw[q - 1], ww[q]);
-        }
-        const float pres_med = mul(0.5f, cu[point_count - 1]);
+#pragma unroll
+        for (int q = 0; q < 9; ++q)
+            if ((unsigned)q >= n) { fu[q] = 0.f; fv[q] = 0.f; fw[q] = 0.f; wt[q] = 0.f; }
+        float tot;
         int32_t c0, c1, c2;
-        ru = median_pick(fu, cu, pres_med, &c0);
-        rv = median_pick(fv, cv, pres_med, &c1);
-        rw = median_pick(fw, cw, pres_med, &c2);
+        ru = median9(fu, wt, n, -1.f, &tot, &c0);
+        const float pres_med = mul(0.5f, tot);   // half of u's total, for all three (:1097)
+        rv = median9(fv, wt, n, pres_med, &tot, &c1);
+        rw = median9(fw, wt, n, pres_med, &tot, &c2);
         if (sel) { sel[index] = c0; sel[g.N + index] = c1; sel[2 * g.N + index] = c2; }
     } else {
         ru = S.du[index];

@@ -78,6 +78,21 @@ struct Carver {
 
 namespace pdflow {
 
+// Waits for the handle's stream and reports (then clears) a device-side
+// timeout recorded by a bounded wait.
+int check_status(pdflow_solver* s)
+{
+    unsigned st = 0;
+    CUDA_TRY(cudaMemcpyAsync(&st, s->status, sizeof st, cudaMemcpyDeviceToHost, s->stream), "status read");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
+    if (st != 0) {
+        CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof st, s->stream), "status reset");
+        CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
+        return set_error(PDFLOW_ERR_TIMEOUT, "a bounded device-side wait gave up (iteration neighbour sync)");
+    }
+    return PDFLOW_OK;
+}
+
 void carve_solver(pdflow_solver* s, char* base, size_t* used)
 {
     Carver cv{base, 0, base == nullptr};
@@ -104,6 +119,9 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     LevelSol& O = s->sol;
     float** op[] = {&O.du, &O.dv, &O.dw, &O.pd, &O.puu, &O.puv, &O.pvu, &O.pvv, &O.pwu, &O.pwv};
     for (float** p : op) *p = cv.plane(N);
+    for (float*& p : s->alt) p = cv.plane(N);
+    s->flags = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 1024));
+    s->status = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 4));
     s->dx = cv.plane(N);
     s->dy = cv.plane(N);
     s->dz = cv.plane(N);
@@ -142,12 +160,44 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st)
         CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
         CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
         const unsigned iters = s->prm.num_max_iter[i];
-        for (unsigned it = 0; it < iters; ++it) {
-            CUDA_TRY(launch_dual(g, s->L, s->S, p, st), "dual launch");
-            CUDA_TRY(launch_primal(g, s->L, s->S, p, it + 1 == iters, o.dep, st), "primal launch");
+        State fin = s->S;   // where the final duals end up
+        if (s->iter_form == 1 && iters > 0) {
+            IterArgs a{};
+            a.g = g;
+            a.L = s->L;
+            a.du = s->S.du;
+            a.dv = s->S.dv;
+            a.dw = s->S.dw;
+            float* b0[10] = {s->S.dua, s->S.dva, s->S.dwa, s->S.pd, s->S.puu, s->S.puv, s->S.pvu, s->S.pvv,
+                             s->S.pwu, s->S.pwv};
+            for (int k = 0; k < 3; ++k) {
+                a.acc[0][k] = b0[k];
+                a.acc[1][k] = s->alt[k];
+            }
+            for (int k = 0; k < 7; ++k) {
+                a.p_[0][k] = b0[3 + k];
+                a.p_[1][k] = s->alt[3 + k];
+            }
+            a.p = p;
+            a.depth_old = o.dep;
+            a.iters = iters;
+            a.flags = s->flags;
+            a.status = s->status;
+            const IterPlan pl = plan_iterate(g, s->num_sms);
+            if (pl.smem_bytes > iterate_smem_limit()) return set_error(PDFLOW_ERR_ARG, "level slab exceeds shared memory");
+            CUDA_TRY(launch_iterate(pl, a, st), "iteration launch");
+            if (iters & 1) {   // the final duals are in the second buffer
+                float** fp[7] = {&fin.pd, &fin.puu, &fin.puv, &fin.pvu, &fin.pvv, &fin.pwu, &fin.pwv};
+                for (int k = 0; k < 7; ++k) *fp[k] = s->alt[3 + k];
+            }
+        } else {
+            for (unsigned it = 0; it < iters; ++it) {
+                CUDA_TRY(launch_dual(g, s->L, s->S, p, st), "dual launch");
+                CUDA_TRY(launch_primal(g, s->L, s->S, p, it + 1 == iters, o.dep, st), "primal launch");
+            }
         }
         if (iters == 0) CUDA_TRY(launch_saturate(g, s->L, s->S, o.dep, st), "saturate launch");
-        CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, s->S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
+        CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
                  "median launch");
     }
     return PDFLOW_OK;
@@ -190,10 +240,18 @@ int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_p
     CUDA_TRY(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
     if (!(prop.major == 10 && prop.minor == 3))
         return set_error(PDFLOW_ERR_NO_DEVICE, "this library is built for sm_103a (GB300) only");
+    {
+        static bool prepared = false;
+        if (!prepared) {
+            CUDA_TRY(prepare_iterate(), "kernel attributes");
+            prepared = true;
+        }
+    }
 
     pdflow_solver* s = new (std::nothrow) pdflow_solver();
     if (!s) return set_error(PDFLOW_ERR_OOM, "host allocation");
     s->device = dev;
+    s->num_sms = prop.multiProcessorCount;
     s->rows = rows;
     s->cols = cols;
     s->width = width;
@@ -314,8 +372,7 @@ int pdflow_read_flow(pdflow_solver* s, float* dx, float* dy, float* dz)
     CUDA_TRY(cudaMemcpyAsync(dx, s->dx, n, cudaMemcpyDeviceToHost, s->stream), "D2H dx");
     CUDA_TRY(cudaMemcpyAsync(dy, s->dy, n, cudaMemcpyDeviceToHost, s->stream), "D2H dy");
     CUDA_TRY(cudaMemcpyAsync(dz, s->dz, n, cudaMemcpyDeviceToHost, s->stream), "D2H dz");
-    CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
-    return PDFLOW_OK;
+    return check_status(s);
 }
 
 int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, const float** dz)
@@ -330,8 +387,7 @@ int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, con
 int pdflow_synchronize(pdflow_solver* s)
 {
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
-    CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
-    return PDFLOW_OK;
+    return check_status(s);
 }
 
 int pdflow_set_stream(pdflow_solver* s, void* stream)

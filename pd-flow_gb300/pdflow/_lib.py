@@ -57,6 +57,7 @@ _SIGNATURES = {
     "pdflow_last_error": (ctypes.c_char_p, []),
     "pdflow_version": (ctypes.c_char_p, []),
     "pdflow_debug_solve": (ctypes.c_int, [vp, DUMP_FN, vp]),
+    "pdflow_set_iteration_form": (ctypes.c_int, [vp, ctypes.c_int]),
     "pdflow_stage_median": (ctypes.c_int, [u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
 }
 
@@ -118,12 +119,13 @@ class Solver:
     freeGPUMemory."""
 
     def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
-                 use_graph: bool = True):
+                 use_graph: bool = True, iteration_form: int = 1):
         self.rows, self.width, self.height = rows, width, height
         self.cols = rows * 320 // 240
         self.params = params
         self._h = None
         self._use_graph = use_graph
+        self._iter_form = iteration_form
         self.dxp = self.dyp = self.dzp = None
 
     # -- reference-shaped API --------------------------------------------------
@@ -134,6 +136,7 @@ class Solver:
         check(lib.pdflow_create(self.rows, self.width, self.height, p, ctypes.byref(h)), "pdflow_create")
         self._h = h
         check(lib.pdflow_set_graph_mode(h, int(self._use_graph)), "pdflow_set_graph_mode")
+        check(lib.pdflow_set_iteration_form(h, int(self._iter_form)), "pdflow_set_iteration_form")
         n = self.rows * self.cols
         self.dxp, self.dyp, self.dzp = (np.zeros(n, np.float32) for _ in range(3))
         return self

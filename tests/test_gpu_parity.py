@@ -25,8 +25,8 @@ def _lib(built_lib):
     return built_lib
 
 
-def solve(g, rows, w, h, raw=True, graph=True, debug=False):
-    s = Solver(rows, w, h, use_graph=graph).initializeCUDA()
+def solve(g, rows, w, h, raw=True, graph=True, debug=False, form=1):
+    s = Solver(rows, w, h, use_graph=graph, iteration_form=form).initializeCUDA()
     try:
         if raw:
             s.loadRGBDFrames(g["i1"], g["z1"], g["i2"], g["z2"])
@@ -186,6 +186,18 @@ def test_solve_is_deterministic(golden_qvga):
 def test_graph_and_stream_forms_agree(golden_qvga):
     a = solve(golden_qvga, 120, 320, 240, graph=True)
     b = solve(golden_qvga, 120, 320, 240, graph=False)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+@pytest.mark.parametrize("fixture,rows,w,h", [CASES[0], CASES[2]])
+def test_iteration_forms_agree(fixture, rows, w, h):
+    """One launch per level's iterations (slab-persistent kernel) and two
+    kernels per iteration give the same bits."""
+    from conftest import load_golden
+    g = load_golden(fixture)
+    a = solve(g, rows, w, h, form=1)
+    b = solve(g, rows, w, h, form=0)
     for x, y in zip(a, b):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
 
