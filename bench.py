@@ -1,0 +1,401 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 PD-Flow solver (one JSON line on stdout).
+
+Workload: VGA scene flow, rows = 480 (640x480 frames, 6 pyramid levels,
+25..100 iterations), seeded synthetic RGB-D pairs (textured plane plus six
+boxes/spheres with rigid motions, depth noise and 2 % holes).  A step is one
+pass of the hot path over one batch: push both frames of every pair (device
+decode + Gaussian pyramid) and the full coarse-to-fine solve.
+
+  value      batched VGA pairs/s, frames resident in HBM (per-step CUDA events
+             on the solver's stream; the batch's working set, ~90 MB per pair,
+             is far larger than L2, so no flush is needed)
+  e2e        the same through the public C ABI from pinned host buffers: raw
+             frames host->device, solve, flow device->host, every step
+  plain      one pair at a time (the plain single-pair solver), L2 flushed
+             before every step; pairs/s and p50/p99 latency
+  roofline   the dominant kernel: the finest level's iterations, timed alone
+  cpu_baseline / --impl reference
+             the FP32 C/OpenMP restatement of the reference (oracle/) on the
+             host cores, on a bounded sample of the same workload
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "pd-flow_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "VGA pairs/s & p99 ms, learned+batched vs plain on one GB300 at EPE<=1mm"
+ROWS, WIDTH, HEIGHT = 480, 640, 480
+ALG_BYTES_PER_PX_ITER = 148       # 13 state floats read + 11 level constants read + 13 state floats written
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_workload(n_distinct: int, batch: int):
+    from pdflow import scenes
+    pairs = [scenes.make_pair(1000 + k, vga=True, n_objects=6) for k in range(n_distinct)]
+    idx = [k % n_distinct for k in range(batch)]
+    stack = lambda j: np.ascontiguousarray(np.stack([pairs[i][j] for i in idx]))
+    return stack(0), stack(1), stack(2), stack(3)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# host-core baseline (the oracle's FP32 OpenMP restatement)
+# ---------------------------------------------------------------------------
+def cpu_baseline(min_seconds: float = 10.0):
+    from oracle import oracle
+    from pdflow import scenes
+    i1, z1, i2, z2 = scenes.make_pair(1000, vga=True, n_objects=6)
+    I1, Z1 = scenes.decode(i1, z1)
+    I2, Z2 = scenes.decode(i2, z2)
+    oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")   # warm (page-in, OpenMP pool)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")
+        n += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": n / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
+            "sample": f"{n} VGA pairs (rows=480) solved by the FP32 OpenMP oracle in {dt:.1f} s"}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle
+    from pdflow import scenes
+    i1, z1, i2, z2 = scenes.make_pair(1000, vga=True, n_objects=6)
+    I1, Z1 = scenes.decode(i1, z1)
+    I2, Z2 = scenes.decode(i2, z2)
+    for _ in range(args.warmup):
+        oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = args.steps / total
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "VGA scene flow rows=480, one pair per step (reference has no GPU-free batch form)",
+                       "rows": ROWS, "image": f"{WIDTH}x{HEIGHT}", "pairs_per_step": 1},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} VGA pairs, FP32 C/OpenMP restatement of pdflow_cudalib.cu"},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "p50_ms": 1000 * statistics.median(times), "p99_ms": 1000 * float(np.quantile(times, 0.99))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-iteration DRAM bytes of the finest level's iteration kernels from a
+    committed ncu summary (profiles/roofline_traffic.json), else None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def ours(args):
+    import torch
+    from pdflow import BatchSolver, Solver, _lib
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = _lib.load()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    B, K, W = args.batch, args.steps, args.warmup
+    log(f"[rank {rank}] generating {min(B, 16)} distinct VGA pairs for a batch of {B}")
+    i1, z1, i2, z2 = make_workload(min(B, 16), B)
+
+    # ---------------- batched, frames resident in HBM ----------------
+    b = BatchSolver(ROWS, WIDTH, HEIGHT, B)
+    _lib.check(lib.pdflow_set_stream(b.handle, ctypes.c_void_p(stream.cuda_stream)), "pdflow_set_stream")
+    d = [torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).to(dev) for a in (i1, z1, i2, z2)]
+
+    def step():
+        b.push_raw_device(B, d[0].data_ptr(), d[1].data_ptr())
+        b.push_raw_device(B, d[2].data_ptr(), d[3].data_ptr())
+        b.solve(B)
+
+    with torch.cuda.stream(stream):
+        for _ in range(W):
+            step()
+    b.synchronize()
+    cfg_launch = ctypes.c_uint()
+    _lib.check(lib.pdflow_last_solve_launches(b.handle, ctypes.byref(cfg_launch)), "launch count")
+    pyr_levels = 6
+    launches_per_step = 2 * pyr_levels + cfg_launch.value      # 2 pushes x (decode + 5 pyramid levels) + solve
+    if ws > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    t_all0, t_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        t_all0.record(stream)
+        for k in range(K):
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        t_all1.record(stream)
+    b.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(e) for a, e in ev]
+    total_ms = t_all0.elapsed_time(t_all1)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * B * K / (total_ms / 1000.0)
+
+    # ---------------- roofline: the finest level's iterations ----------------
+    hbm_peak, peak_kind = measured_peaks()
+    R_f, C_f = ROWS, ROWS * 4 // 3
+    iters = 10
+    ms = ctypes.c_float()
+    with torch.cuda.stream(stream):
+        _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
+        _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
+    alg_bytes = ALG_BYTES_PER_PX_ITER * B * R_f * C_f          # per iteration (one dual + one primal launch)
+    achieved = alg_bytes / (ms.value / iters / 1000.0) / 1e9
+    trf = profiled_traffic()
+    traffic = None
+    if trf and trf.get("rows") == ROWS and trf.get("bytes_per_px_iter"):
+        traffic = float(trf["bytes_per_px_iter"]) * B * R_f * C_f
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": traffic, "peak_kind": peak_kind,
+                "kernel": f"finest-level iteration (480x640, {B} pairs; dual+primal per iteration)",
+                "algorithmic_bytes_per_px_iter": ALG_BYTES_PER_PX_ITER,
+                "ms_per_iteration": ms.value / iters}
+
+    # ---------------- e2e through the public API, host buffers ----------------
+    h = [torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).pin_memory() for a in (i1, z1, i2, z2)]
+    N = ROWS * (ROWS * 4 // 3)
+    hout = [torch.empty((B, N), dtype=torch.float32).pin_memory() for _ in range(3)]
+
+    def e2e_step():
+        _lib.check(lib.pdflow_push_frames_u16(b.handle, B, ctypes.c_void_p(h[0].data_ptr()),
+                                              ctypes.c_void_p(h[1].data_ptr())), "push")
+        _lib.check(lib.pdflow_push_frames_u16(b.handle, B, ctypes.c_void_p(h[2].data_ptr()),
+                                              ctypes.c_void_p(h[3].data_ptr())), "push")
+        _lib.check(lib.pdflow_solve_batch(b.handle, B), "solve")
+        _lib.check(lib.pdflow_read_flow_batch(b.handle, B, *[ctypes.c_void_p(x.data_ptr()) for x in hout]), "read")
+
+    for _ in range(min(W, 2)):
+        e2e_step()
+    ke = max(3, K // 2)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t0.record(stream)
+        for _ in range(ke):
+            e2e_step()
+        t1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1)
+    e2e = {"value": ws * B * ke / (e2e_ms / 1000.0), "unit": "pairs/s",
+           "h2d_bytes_per_step": int(2 * B * WIDTH * HEIGHT * 3), "d2h_bytes_per_step": int(3 * B * N * 4)}
+    # parity spot check of the batch against a single-pair solve of pair 0
+    b.close()
+
+    # ---------------- plain single-pair solver ----------------
+    s = Solver(ROWS, WIDTH, HEIGHT).initializeCUDA()
+    _lib.check(lib.pdflow_set_stream(s.handle, ctypes.c_void_p(stream.cuda_stream)), "pdflow_set_stream")
+    ds = [x[0].contiguous() for x in d]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
+
+    def single_step():
+        _lib.check(lib.pdflow_push_frame_u16_device(s.handle, ctypes.c_void_p(ds[0].data_ptr()),
+                                                    ctypes.c_void_p(ds[1].data_ptr())), "push")
+        _lib.check(lib.pdflow_push_frame_u16_device(s.handle, ctypes.c_void_p(ds[2].data_ptr()),
+                                                    ctypes.c_void_p(ds[3].data_ptr())), "push")
+        _lib.check(lib.pdflow_solve(s.handle), "solve")
+
+    with torch.cuda.stream(stream):
+        for _ in range(W):
+            single_step()
+    torch.cuda.synchronize()
+    ns = max(20, K)
+    sev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(ns)]
+    with torch.cuda.stream(stream):
+        for k in range(ns):
+            flush.zero_()
+            sev[k][0].record(stream)
+            single_step()
+            sev[k][1].record(stream)
+    torch.cuda.synchronize()
+    single_ms = [a.elapsed_time(e) for a, e in sev]
+    s.freeGPUMemory()
+    plain = {"pairs_s": 1000.0 / statistics.mean(single_ms), "p50_ms": statistics.median(single_ms),
+             "p99_ms": float(np.quantile(single_ms, 0.99)), "steps": ns, "l2": "256 MB flush before each step"}
+
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"VGA scene flow, rows=480 (640x480, 6 levels, 25..100 iterations), "
+                                   f"batch of {B} pairs per step", "rows": ROWS, "image": f"{WIDTH}x{HEIGHT}",
+                       "pairs_per_step_per_gpu": B, "parallelism": f"replicas x{ws}", "learned_warm_start": False,
+                       "l2": "batch working set far above L2 (no flush); plain single pair: L2 flushed per step",
+                       "distinct_scenes": min(B, 16)},
+            "batched": {"pairs_s": value, "p50_ms_per_batch": statistics.median(step_ms),
+                        "p99_ms_per_batch": float(np.quantile(step_ms, 0.99))},
+            "plain": plain, "p99_ms": plain["p99_ms"], "e2e": e2e, "roofline": roofline,
+            "gpu_launches": launches_per_step * K, "clocks": clocks}
+    if rank == 0:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        except Exception as ex:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(ex)}
+        line["reference_cuda"] = reference_cuda_timing()
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def reference_cuda_timing():
+    """The reference's own CUDA path (its device code from oracle/_ref, the
+    host sequence replayed by oracle/ref/refharness.c) on the same GPU."""
+    try:
+        from oracle import refharness
+        if not refharness.available():
+            return None
+        from pdflow import scenes
+        i1, z1, i2, z2 = scenes.make_pair(1000, vga=True, n_objects=6)
+        I1, Z1 = scenes.decode(i1, z1)
+        I2, Z2 = scenes.decode(i2, z2)
+        r = refharness.RefSolver(ROWS, WIDTH, HEIGHT)
+        r.time_pairs(I1, Z1, I2, Z2, 2)
+        ms = r.time_pairs(I1, Z1, I2, Z2, 10)
+        r.close()
+        return {"pairs_s": 1000.0 / ms, "ms_per_pair": ms, "sample": "10 VGA pairs, host-timed, incl. its per-level "
+                "cudaMalloc/cudaFree and H2D/D2H copies"}
+    except Exception as ex:
+        return {"error": str(ex)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -119,6 +119,42 @@ int pdflow_get_config(const pdflow_solver* s, unsigned* rows, unsigned* cols, un
  * 1 = the whole solve replayed as one captured CUDA graph (default). */
 int pdflow_set_graph_mode(pdflow_solver* s, int use_graph);
 
+/* ---- Batches: many independent pairs of one configuration in one handle ----
+ * The reference solves one pair per object; a batch handle holds `max_pairs`
+ * solver states in one device allocation and runs the same coarse-to-fine
+ * schedule for pairs [0, n) with one launch per kernel for all of them.  Each
+ * pair's result equals a single-pair solve of the same frames, bit for bit.
+ * Multi-pair buffers are contiguous arrays of per-pair buffers with the
+ * layouts of the single-pair calls above. */
+
+/* Creates a handle for up to max_pairs pairs (pdflow_create == max_pairs 1). */
+int pdflow_create_batch(unsigned rows, unsigned width, unsigned height, const pdflow_params* params,
+                        unsigned max_pairs, pdflow_solver** out);
+
+/* Pushes one frame for each of pairs [0, n): float column-major staging
+ * buffers [n][width*height] (as pdflow_push_frame). */
+int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float* Z);
+
+/* Pushes raw frames [n][height][width] uint8 / uint16 (as pdflow_push_frame_u16). */
+int pdflow_push_frames_u16(pdflow_solver* s, unsigned n, const uint8_t* intensity, const uint16_t* depth);
+
+/* Same with device pointers (contiguous [n][height][width]). */
+int pdflow_push_frames_u16_device(pdflow_solver* s, unsigned n, const uint8_t* d_intensity,
+                                  const uint16_t* d_depth);
+
+/* Solves pairs [0, n) (asynchronous on the handle's stream). */
+int pdflow_solve_batch(pdflow_solver* s, unsigned n);
+
+/* Copies the motion fields of pairs [0, n) to host arrays [n][rows*cols]. */
+int pdflow_read_flow_batch(pdflow_solver* s, unsigned n, float* dx, float* dy, float* dz);
+
+/* Capacity of a handle and the byte distance between consecutive pairs'
+ * device buffers (pdflow_flow_device returns pair 0's planes). */
+int pdflow_batch_info(const pdflow_solver* s, unsigned* max_pairs, size_t* pair_stride_bytes);
+
+/* Device memory held by the handle, in bytes (0 for NULL). */
+size_t pdflow_device_bytes(const pdflow_solver* s);
+
 /* Human-readable text of the last error on this thread. */
 const char* pdflow_last_error(void);
 

@@ -30,6 +30,17 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
  * fused).  Both give the same bits. */
 int pdflow_set_iteration_form(pdflow_solver* s, int form);
 
+/* Number of kernels the last pdflow_solve / pdflow_solve_batch launched
+ * (graph replays count the kernels of the captured solve). */
+int pdflow_last_solve_launches(const pdflow_solver* s, unsigned* count);
+
+/* Runs `iters` iterations of coarse-to-fine level `level` (0 = coarsest) for
+ * pairs [0, n) in the launch form pdflow_solve uses, on the handle's stream,
+ * after a solve has left that level's constants in place, and returns the
+ * elapsed device time (CUDA events on that stream) in *ms.  The handle's state
+ * is overwritten; push frames again before the next solve. */
+int pdflow_time_level_iterations(pdflow_solver* s, unsigned n, unsigned level, unsigned iters, float* ms);
+
 /* The 3x3 weighted median of filterSolution (pdflow_cudalib.cu:1040-1148) on
  * caller planes (device pointers, R*C floats, column-major).  `sel` (device,
  * 3*R*C int32, may be NULL) receives, per component, the bracketing index the

@@ -118,14 +118,36 @@ int pdflow_set_iteration_form(pdflow_solver* s, int form)
     if (!s || (form != 0 && form != 1)) return PDFLOW_ERR_ARG;
     if (s->iter_form != form) {
         cudaStreamSynchronize(s->stream);
-        for (int k = 0; k < 2; ++k)
-            if (s->solve_graph[k]) {
-                cudaGraphExecDestroy(s->solve_graph[k]);
-                s->solve_graph[k] = nullptr;
-            }
-        s->iter_form = form;
+        s->iter_form = form;   // graphs are cached per iteration form
     }
     return PDFLOW_OK;
+}
+
+int pdflow_last_solve_launches(const pdflow_solver* s, unsigned* count)
+{
+    if (!s || !count) return PDFLOW_ERR_ARG;
+    *count = s->launches;
+    return PDFLOW_OK;
+}
+
+int pdflow_time_level_iterations(pdflow_solver* s, unsigned n, unsigned level, unsigned iters, float* ms)
+{
+    if (!s || !ms || n == 0 || n > s->batch || level >= s->ctf_levels || iters == 0) return PDFLOW_ERR_ARG;
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) return PDFLOW_ERR_CUDA;
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return PDFLOW_ERR_CUDA;
+    }
+    cudaEventRecord(a, s->stream);
+    int rc = enqueue_level_iterations(s, s->stream, n, level, iters);
+    cudaEventRecord(b, s->stream);
+    cudaError_t e = cudaEventSynchronize(b);
+    if (rc == PDFLOW_OK && e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc != PDFLOW_OK) return rc;
+    return e == cudaSuccess ? PDFLOW_OK : fail("timing", e);
 }
 
 int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const float* ddt, const float* du,
@@ -133,7 +155,7 @@ int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const fl
                         void* stream)
 {
     if (!depth_old || !ddt || !du || !dv || !dw || !du_l || !dv_l || !dw_l || R < 2 || C < 2) return PDFLOW_ERR_ARG;
-    LevelGeom g{R, C, R * C};
+    LevelGeom g{R, C, R * C};  // one pair, no stride
     PyrLevel o{nullptr, const_cast<float*>(depth_old), nullptr, nullptr};
     LevelConsts L{};
     L.ddt = const_cast<float*>(ddt);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/pdflow.h"
 #include "pdflow_iterate.cuh"
 #include "pdflow_kernels.cuh"
@@ -34,13 +36,24 @@ struct pdflow_solver {
     float* dy = nullptr;
     float* dz = nullptr;
     int use_graph = 1;
-    cudaGraphExec_t solve_graph[2] = {nullptr, nullptr};  // one per old/new slot assignment
+    unsigned batch = 1;                  // pairs the arena holds
+    size_t pair_stride = 0;              // bytes between pair k and pair k+1 buffers
+    unsigned launches = 0;               // kernel launches of the last enqueued solve
+    struct GraphEntry {
+        int slot;
+        unsigned pairs;
+        int form;
+        cudaGraphExec_t exec;
+        unsigned launches;
+    };
+    std::vector<GraphEntry> graphs;      // captured solves, per (slot, pair count, iteration form)
 };
 
 namespace pdflow {
 void carve_solver(pdflow_solver* s, char* base, size_t* used);
-int enqueue_pyramid(pdflow_solver* s, cudaStream_t st);
-int enqueue_solve(pdflow_solver* s, cudaStream_t st);
+int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs);
+int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs);
+int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);
 int check_status(pdflow_solver* s);
-LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image);
+LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, unsigned pairs = 1);
 }  // namespace pdflow

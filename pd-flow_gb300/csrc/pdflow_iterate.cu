@@ -79,6 +79,19 @@ template <int kMode>
 __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
 {
     extern __shared__ float sm[];
+    if (kMode != kIterGrid && blockIdx.y > 0) {
+        // batch: pair blockIdx.y of a strided arena
+        const size_t po = (size_t)blockIdx.y * a.g.pstride;
+        a.L = at(a.L, po);
+        a.du = at(a.du, po);
+        a.dv = at(a.dv, po);
+        a.dw = at(a.dw, po);
+        for (int q = 0; q < 2; ++q) {
+            for (int k = 0; k < 3; ++k) a.acc[q][k] = at(a.acc[q][k], po);
+            for (int k = 0; k < 7; ++k) a.p_[q][k] = at(a.p_[q][k], po);
+        }
+        a.depth_old = at(a.depth_old, po);
+    }
     const unsigned R = a.g.R, C = a.g.C;
     const unsigned nb = gridDim.x, b = blockIdx.x;
     const unsigned u0 = (unsigned)((unsigned long long)b * C / nb);
@@ -318,7 +331,7 @@ cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st)
     a.smem_plane = pl.smem_plane;
     a.smem_state_plane = pl.smem_state_plane;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(pl.ctas);
+    cfg.gridDim = dim3(pl.ctas, pl.mode == kIterGrid ? 1 : a.g.pairs);
     cfg.blockDim = dim3(kIterThreads);
     cfg.dynamicSmemBytes = pl.smem_bytes;
     cfg.stream = st;

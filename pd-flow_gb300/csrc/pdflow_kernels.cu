@@ -33,8 +33,11 @@ __device__ __forceinline__ void write_xy(PyrLevel out, unsigned R, unsigned C, u
 // transpose through a 32x33 shared tile so that both sides are coalesced).
 __global__ void __launch_bounds__(1024) k_decode_u16(const uint8_t* __restrict__ img,
                                                      const uint16_t* __restrict__ depth, unsigned W, unsigned H,
-                                                     PyrLevel out, float fovh)
+                                                     PyrLevel out, float fovh, size_t pstride)
 {
+    img += (size_t)blockIdx.z * W * H;
+    depth += (size_t)blockIdx.z * W * H;
+    out = at(out, (size_t)blockIdx.z * pstride);
     __shared__ float sc[32][33];
     __shared__ float sz[32][33];
     const unsigned x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
@@ -58,8 +61,12 @@ __global__ void __launch_bounds__(1024) k_decode_u16(const uint8_t* __restrict__
 }
 
 __global__ void k_pyr_level0(const float* __restrict__ I, const float* __restrict__ Z, unsigned R, unsigned C,
-                             PyrLevel out, float fovh)
+                             PyrLevel out, float fovh, size_t pstride)
 {
+    const size_t po = (size_t)blockIdx.y * pstride;
+    I = at(I, po);
+    Z = at(Z, po);
+    out = at(out, po);
     const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= R * C) return;
     const unsigned v = idx % R, u = idx / R;
@@ -69,8 +76,11 @@ __global__ void k_pyr_level0(const float* __restrict__ I, const float* __restric
     write_xy(out, R, C, v, u, idx, z, fovh);
 }
 
-__global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh)
+__global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, size_t pstride)
 {
+    const size_t po = (size_t)blockIdx.y * pstride;
+    prev = at(prev, po);
+    out = at(out, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
     if (index >= R * C) return;
     const unsigned v = index % R, u = index / R;
@@ -136,6 +146,12 @@ __global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, 
 // contribute exactly zero and are skipped), followed by computeRij (:725-779).
 __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    cs = at(cs, po);
+    o = at(o, po);
+    n = at(n, po);
+    L = at(L, po);
+    S = at(S, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
     if (index >= g.N) return;
     const unsigned R = g.R, C = g.C;
@@ -222,6 +238,9 @@ __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, P
 // computeImGradients (pdflow_cudalib.cu:574-627) on the new frame.
 __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    n = at(n, po);
+    L = at(L, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
     if (index >= g.N) return;
     const unsigned R = g.R, C = g.C;
@@ -257,6 +276,10 @@ __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 // performWarping (pdflow_cudalib.cu:629-652) + computeMu/computeStepSizes (:781-808).
 __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    o = at(o, po);
+    n = at(n, po);
+    L = at(L, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
     if (index >= g.N) return;
     const unsigned R = g.R, C = g.C;
@@ -296,6 +319,9 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
 // ---------------------------------------------------------------------------
 __global__ void k_dual(LevelGeom g, LevelConsts L, State S, Params p)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    L = at(L, po);
+    S = at(S, po);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.N) return;
     const unsigned R = g.R, C = g.C;
@@ -318,6 +344,10 @@ __global__ void k_dual(LevelGeom g, LevelConsts L, State S, Params p)
 
 __global__ void k_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    L = at(L, po);
+    S = at(S, po);
+    depth_old = at(depth_old, po);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.N) return;
     const unsigned R = g.R, C = g.C;
@@ -346,6 +376,10 @@ __global__ void k_primal(LevelGeom g, LevelConsts L, State S, Params p, bool las
 // saturateVariables alone, for a level scheduled with zero iterations.
 __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    L = at(L, po);
+    S = at(S, po);
+    depth_old = at(depth_old, po);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.N) return;
     float du = S.du[i], dv = S.dv[i], dw = S.dw[i];
@@ -417,6 +451,14 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
 __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, LevelSol out, float* dx,
                          float* dy, float* dz, Params p, int32_t* sel)
 {
+    const size_t po = (size_t)blockIdx.y * g.pstride;
+    o = at(o, po);
+    L = at(L, po);
+    S = at(S, po);
+    out = at(out, po);
+    dx = at(dx, po);
+    dy = at(dy, po);
+    dz = at(dz, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
     if (index >= g.N) return;
     const unsigned R = g.R, C = g.C;
@@ -488,68 +530,71 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
 // Launchers
 // ---------------------------------------------------------------------------
 cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
-                              float fovh, cudaStream_t st)
+                              float fovh, unsigned pairs, size_t pstride, cudaStream_t st)
 {
-    dim3 grid((W + 31) / 32, (H + 31) / 32), block(32, 32);
-    k_decode_u16<<<grid, block, 0, st>>>(img, depth, W, H, out, fovh);
+    dim3 grid((W + 31) / 32, (H + 31) / 32, pairs), block(32, 32);
+    k_decode_u16<<<grid, block, 0, st>>>(img, depth, W, H, out, fovh, pstride);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pyr_level0(const float* I, const float* Z, unsigned R, unsigned C, PyrLevel out, float fovh,
-                              cudaStream_t st)
+                              unsigned pairs, size_t pstride, cudaStream_t st)
 {
-    k_pyr_level0<<<blocks_for(R * C), kBlock, 0, st>>>(I, Z, R, C, out, fovh);
+    k_pyr_level0<<<dim3(blocks_for(R * C), pairs), kBlock, 0, st>>>(I, Z, R, C, out, fovh, pstride);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, cudaStream_t st)
+cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, unsigned pairs,
+                            size_t pstride, cudaStream_t st)
 {
-    k_pyr_down<<<blocks_for(R * C), kBlock, 0, st>>>(prev, R, C, out, fovh);
+    k_pyr_down<<<dim3(blocks_for(R * C), pairs), kBlock, 0, st>>>(prev, R, C, out, fovh, pstride);
     return cudaGetLastError();
 }
+
+static dim3 level_grid(const LevelGeom& g) { return dim3(blocks_for(g.N), g.pairs); }
 
 cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel old_l, PyrLevel new_l,
                               LevelConsts L, State S, cudaStream_t st)
 {
-    k_level_init<<<blocks_for(g.N), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S);
+    k_level_init<<<level_grid(g), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S);
     return cudaGetLastError();
 }
 
 cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st)
 {
-    k_im_gradients<<<blocks_for(g.N), kBlock, 0, st>>>(g, new_l, L);
+    k_im_gradients<<<level_grid(g), kBlock, 0, st>>>(g, new_l, L);
     return cudaGetLastError();
 }
 
 cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p, cudaStream_t st)
 {
-    k_warp_steps<<<blocks_for(g.N), kBlock, 0, st>>>(g, old_l, new_l, L, p);
+    k_warp_steps<<<level_grid(g), kBlock, 0, st>>>(g, old_l, new_l, L, p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_dual(LevelGeom g, LevelConsts L, State S, Params p, cudaStream_t st)
 {
-    k_dual<<<blocks_for(g.N), kBlock, 0, st>>>(g, L, S, p);
+    k_dual<<<level_grid(g), kBlock, 0, st>>>(g, L, S, p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old,
                           cudaStream_t st)
 {
-    k_primal<<<blocks_for(g.N), kBlock, 0, st>>>(g, L, S, p, last, depth_old);
+    k_primal<<<level_grid(g), kBlock, 0, st>>>(g, L, S, p, last, depth_old);
     return cudaGetLastError();
 }
 
 cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old, cudaStream_t st)
 {
-    k_saturate<<<blocks_for(g.N), kBlock, 0, st>>>(g, L, S, depth_old);
+    k_saturate<<<level_grid(g), kBlock, 0, st>>>(g, L, S, depth_old);
     return cudaGetLastError();
 }
 
 cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out, float* dx,
                           float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st)
 {
-    k_median<<<blocks_for(g.N), kBlock, 0, st>>>(g, finest, old_l, L, S, out, dx, dy, dz, p, sel);
+    k_median<<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, out, dx, dy, dz, p, sel);
     return cudaGetLastError();
 }
 

@@ -34,9 +34,47 @@ struct LevelSol {
     float *du, *dv, *dw, *pd, *puu, *puv, *pvu, *pvv, *pwu, *pwv;
 };
 
+// Level size plus the batch view: `pairs` solves share one arena, pair k's
+// buffers sit k * pstride bytes after pair 0's (every pointer handed to a
+// kernel is pair 0's; kernels take the pair from their grid's y index).
 struct LevelGeom {
     unsigned R, C, N;
+    unsigned pairs = 1;
+    size_t pstride = 0;
 };
+
+template <class T>
+__host__ __device__ __forceinline__ T* at(T* p, size_t off)
+{
+    return p ? reinterpret_cast<T*>(reinterpret_cast<uintptr_t>(p) + off) : p;
+}
+__host__ __device__ __forceinline__ PyrLevel at(PyrLevel a, size_t o)
+{
+    return PyrLevel{at(a.col, o), at(a.dep, o), at(a.xx, o), at(a.yy, o)};
+}
+__host__ __device__ __forceinline__ LevelConsts at(LevelConsts L, size_t o)
+{
+    LevelConsts r;
+    r.ri = at(L.ri, o); r.rj = at(L.rj, o); r.ri2 = at(L.ri2, o); r.rj2 = at(L.rj2, o);
+    r.dcu_aux = at(L.dcu_aux, o); r.dcv_aux = at(L.dcv_aux, o); r.ddu_aux = at(L.ddu_aux, o);
+    r.ddv_aux = at(L.ddv_aux, o);
+    r.dct = at(L.dct, o); r.dcu = at(L.dcu, o); r.dcv = at(L.dcv, o); r.ddt = at(L.ddt, o); r.ddu = at(L.ddu, o);
+    r.ddv = at(L.ddv, o);
+    r.mu = at(L.mu, o); r.du_prev = at(L.du_prev, o); r.dv_prev = at(L.dv_prev, o);
+    r.spd = at(L.spd, o); r.spuvx = at(L.spuvx, o); r.spuvy = at(L.spuvy, o); r.spwx = at(L.spwx, o);
+    r.spwy = at(L.spwy, o); r.tu = at(L.tu, o); r.tv = at(L.tv, o); r.tw = at(L.tw, o);
+    return r;
+}
+__host__ __device__ __forceinline__ State at(State S, size_t o)
+{
+    return State{at(S.du, o), at(S.dv, o), at(S.dw, o), at(S.dua, o), at(S.dva, o), at(S.dwa, o), at(S.pd, o),
+                 at(S.puu, o), at(S.puv, o), at(S.pvu, o), at(S.pvv, o), at(S.pwu, o), at(S.pwv, o)};
+}
+__host__ __device__ __forceinline__ LevelSol at(LevelSol s, size_t o)
+{
+    return LevelSol{at(s.du, o), at(s.dv, o), at(s.dw, o), at(s.pd, o), at(s.puu, o), at(s.puv, o), at(s.pvu, o),
+                    at(s.pvv, o), at(s.pwu, o), at(s.pwv, o)};
+}
 
 struct Params {
     float lambda_i, lambda_d, mu, fovh;
@@ -44,11 +82,14 @@ struct Params {
 };
 
 // ---- launchers (each returns the launch error) ----
+// Pyramid launchers: `pairs` frames, pair k's arena buffers k * pstride bytes
+// after pair 0's; the raw inputs of launch_decode_u16 are [pairs][H][W].
 cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
-                              float fovh, cudaStream_t st);
+                              float fovh, unsigned pairs, size_t pstride, cudaStream_t st);
 cudaError_t launch_pyr_level0(const float* I, const float* Z, unsigned R, unsigned C, PyrLevel out, float fovh,
-                              cudaStream_t st);
-cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, cudaStream_t st);
+                              unsigned pairs, size_t pstride, cudaStream_t st);
+cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, unsigned pairs,
+                            size_t pstride, cudaStream_t st);
 cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel old_l, PyrLevel new_l,
                               LevelConsts L, State S, cudaStream_t st);
 cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st);

@@ -93,6 +93,9 @@ int check_status(pdflow_solver* s)
     return PDFLOW_OK;
 }
 
+// Carves the arena: `batch` identical per-pair slices (pair k's buffers
+// k * pair_stride bytes after pair 0's) followed by a shared region (raw-frame
+// staging for every pair, progress counters, status word).
 void carve_solver(pdflow_solver* s, char* base, size_t* used)
 {
     Carver cv{base, 0, base == nullptr};
@@ -104,8 +107,6 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
         }
     s->stage_I = cv.plane(Nimg);
     s->stage_Z = cv.plane(Nimg);
-    s->stage_u8 = static_cast<uint8_t*>(cv.bytes(Nimg));
-    s->stage_u16 = static_cast<uint16_t*>(cv.bytes(Nimg * 2));
     const size_t N = size_t(s->rows) * s->cols;
     LevelConsts& L = s->L;
     float** lp[] = {&L.ri, &L.rj, &L.ri2, &L.rj2, &L.dcu_aux, &L.dcv_aux, &L.ddu_aux, &L.ddv_aux, &L.dct,
@@ -120,86 +121,129 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     float** op[] = {&O.du, &O.dv, &O.dw, &O.pd, &O.puu, &O.puv, &O.pvu, &O.pvv, &O.pwu, &O.pwv};
     for (float** p : op) *p = cv.plane(N);
     for (float*& p : s->alt) p = cv.plane(N);
-    s->flags = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 1024));
-    s->status = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 4));
     s->dx = cv.plane(N);
     s->dy = cv.plane(N);
     s->dz = cv.plane(N);
+    cv.off = (cv.off + 255) & ~size_t(255);
+    s->pair_stride = cv.off;
+    cv.off = s->pair_stride * s->batch;
+    s->stage_u8 = static_cast<uint8_t*>(cv.bytes(Nimg * s->batch));
+    s->stage_u16 = static_cast<uint16_t*>(cv.bytes(Nimg * 2 * s->batch));
+    s->flags = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 1024));
+    s->status = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 4));
     *used = cv.off;
 }
 
-int enqueue_pyramid(pdflow_solver* s, cudaStream_t st)
+int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs)
 {
     const int f = s->new_slot;
     for (unsigned l = 1; l < s->pyr_levels; ++l) {
         const unsigned Cl = 640 / (s->cam_mode << l), Rl = 480 / (s->cam_mode << l);
-        CUDA_TRY(launch_pyr_down(s->pyr[f][l - 1], Rl, Cl, s->pyr[f][l], s->prm.fovh, st), "pyramid launch");
+        CUDA_TRY(launch_pyr_down(s->pyr[f][l - 1], Rl, Cl, s->pyr[f][l], s->prm.fovh, pairs, s->pair_stride, st),
+                 "pyramid launch");
     }
     return PDFLOW_OK;
 }
 
-LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image)
+LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, unsigned pairs)
 {
     const unsigned sdiv = 1u << (s->ctf_levels - (i + 1));
     const unsigned Ci = s->cols / sdiv, Ri = s->rows / sdiv;
     if (level_image) *level_image = s->ctf_levels - i + log2u(s->width / s->cols) - 1;
-    return LevelGeom{Ri, Ci, Ri * Ci};
+    LevelGeom g{Ri, Ci, Ri * Ci};
+    g.pairs = pairs;
+    g.pstride = s->pair_stride;
+    return g;
 }
 
-// The kernel sequence of one solve (scene_flow_impair.cpp:103-167), for the
-// current old/new slot assignment.
-int enqueue_solve(pdflow_solver* s, cudaStream_t st)
+// The kernel sequence of one solve (scene_flow_impair.cpp:103-167) for pairs
+// [0, pairs), for the current old/new slot assignment.  A level's iterations
+// run as one launch (k_iterate: one CTA, one cluster, or, for a single pair,
+// the cooperative full grid) or, for a batch of pairs at a level that needs
+// the full grid, as two batched kernels per iteration.
+// Enqueues `iters` iterations of level i for pairs [0, pairs) in the
+// solve's launch form; returns the number of kernels launched via *count.
+// The final duals' buffer is reported in *fin.
+static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom& g, const PyrLevel& o,
+                              unsigned iters, unsigned pairs, State* fin, unsigned* count)
+{
+    Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
+    *fin = s->S;
+    const IterPlan pl = plan_iterate(g, s->num_sms);
+    const bool one_launch = s->iter_form == 1 && iters > 0 && (pairs == 1 || pl.mode != kIterGrid) &&
+                            pl.smem_bytes <= iterate_smem_limit();
+    if (one_launch) {
+        IterArgs a{};
+        a.g = g;
+        a.L = s->L;
+        a.du = s->S.du;
+        a.dv = s->S.dv;
+        a.dw = s->S.dw;
+        float* b0[10] = {s->S.dua, s->S.dva, s->S.dwa, s->S.pd, s->S.puu, s->S.puv, s->S.pvu, s->S.pvv,
+                         s->S.pwu, s->S.pwv};
+        for (int k = 0; k < 3; ++k) {
+            a.acc[0][k] = b0[k];
+            a.acc[1][k] = s->alt[k];
+        }
+        for (int k = 0; k < 7; ++k) {
+            a.p_[0][k] = b0[3 + k];
+            a.p_[1][k] = s->alt[3 + k];
+        }
+        a.p = p;
+        a.depth_old = o.dep;
+        a.iters = iters;
+        a.flags = s->flags;
+        a.status = s->status;
+        CUDA_TRY(launch_iterate(pl, a, st), "iteration launch");
+        *count += 1;
+        if (iters & 1) {   // the final duals are in the second buffer
+            float** fp[7] = {&fin->pd, &fin->puu, &fin->puv, &fin->pvu, &fin->pvv, &fin->pwu, &fin->pwv};
+            for (int k = 0; k < 7; ++k) *fp[k] = s->alt[3 + k];
+        }
+    } else {
+        for (unsigned it = 0; it < iters; ++it) {
+            CUDA_TRY(launch_dual(g, s->L, s->S, p, st), "dual launch");
+            CUDA_TRY(launch_primal(g, s->L, s->S, p, it + 1 == iters, o.dep, st), "primal launch");
+        }
+        *count += 2 * iters;
+    }
+    return PDFLOW_OK;
+}
+
+int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters)
+{
+    unsigned li, cnt = 0;
+    const LevelGeom g = level_geom(s, level, &li, pairs);
+    State fin;
+    return enqueue_iterations(s, st, g, s->pyr[s->new_slot ^ 1][li], iters, pairs, &fin, &cnt);
+}
+
+int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs)
 {
     Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
     const int fn = s->new_slot, fo = fn ^ 1;
+    unsigned count = 0;
     for (unsigned i = 0; i < s->ctf_levels; ++i) {
         unsigned li;
-        const LevelGeom g = level_geom(s, i, &li);
+        const LevelGeom g = level_geom(s, i, &li, pairs);
         const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];
         CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st), "level init launch");
         CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
         CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
+        count += 3;
         const unsigned iters = s->prm.num_max_iter[i];
-        State fin = s->S;   // where the final duals end up
-        if (s->iter_form == 1 && iters > 0) {
-            IterArgs a{};
-            a.g = g;
-            a.L = s->L;
-            a.du = s->S.du;
-            a.dv = s->S.dv;
-            a.dw = s->S.dw;
-            float* b0[10] = {s->S.dua, s->S.dva, s->S.dwa, s->S.pd, s->S.puu, s->S.puv, s->S.pvu, s->S.pvv,
-                             s->S.pwu, s->S.pwv};
-            for (int k = 0; k < 3; ++k) {
-                a.acc[0][k] = b0[k];
-                a.acc[1][k] = s->alt[k];
-            }
-            for (int k = 0; k < 7; ++k) {
-                a.p_[0][k] = b0[3 + k];
-                a.p_[1][k] = s->alt[3 + k];
-            }
-            a.p = p;
-            a.depth_old = o.dep;
-            a.iters = iters;
-            a.flags = s->flags;
-            a.status = s->status;
-            const IterPlan pl = plan_iterate(g, s->num_sms);
-            if (pl.smem_bytes > iterate_smem_limit()) return set_error(PDFLOW_ERR_ARG, "level slab exceeds shared memory");
-            CUDA_TRY(launch_iterate(pl, a, st), "iteration launch");
-            if (iters & 1) {   // the final duals are in the second buffer
-                float** fp[7] = {&fin.pd, &fin.puu, &fin.puv, &fin.pvu, &fin.pvv, &fin.pwu, &fin.pwv};
-                for (int k = 0; k < 7; ++k) *fp[k] = s->alt[3 + k];
-            }
-        } else {
-            for (unsigned it = 0; it < iters; ++it) {
-                CUDA_TRY(launch_dual(g, s->L, s->S, p, st), "dual launch");
-                CUDA_TRY(launch_primal(g, s->L, s->S, p, it + 1 == iters, o.dep, st), "primal launch");
-            }
+        State fin;
+        int rc = enqueue_iterations(s, st, g, o, iters, pairs, &fin, &count);
+        if (rc) return rc;
+        if (iters == 0) {
+            CUDA_TRY(launch_saturate(g, s->L, s->S, o.dep, st), "saturate launch");
+            ++count;
         }
-        if (iters == 0) CUDA_TRY(launch_saturate(g, s->L, s->S, o.dep, st), "saturate launch");
         CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
                  "median launch");
+        ++count;
     }
+    s->launches = count;
     return PDFLOW_OK;
 }
 
@@ -208,6 +252,20 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st)
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+namespace {
+
+int push_common(pdflow_solver* s, unsigned pairs)
+{
+    int rc = enqueue_pyramid(s, s->stream, pairs);
+    if (rc) return rc;
+    if (s->frames < 2) ++s->frames;
+    return PDFLOW_OK;
+}
+
+bool bad_count(const pdflow_solver* s, unsigned n) { return n == 0 || n > s->batch; }
+
+}  // namespace
+
 extern "C" {
 
 int pdflow_default_params(unsigned rows, pdflow_params* p)
@@ -225,7 +283,8 @@ int pdflow_default_params(unsigned rows, pdflow_params* p)
     return PDFLOW_OK;
 }
 
-int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_params* params, pdflow_solver** out)
+int pdflow_create_batch(unsigned rows, unsigned width, unsigned height, const pdflow_params* params,
+                        unsigned max_pairs, pdflow_solver** out)
 {
     if (!out) return set_error(PDFLOW_ERR_ARG, "null output handle");
     *out = nullptr;
@@ -234,6 +293,7 @@ int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_p
         return set_error(PDFLOW_ERR_ARG, "image must be 640x480 or 320x240");
     const unsigned cols = rows * 320 / 240;
     if (cols > width) return set_error(PDFLOW_ERR_ARG, "rows exceed the image resolution");
+    if (max_pairs == 0 || max_pairs > 65535) return set_error(PDFLOW_ERR_ARG, "batch size must be 1..65535");
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     cudaDeviceProp prop;
@@ -256,6 +316,7 @@ int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_p
     s->cols = cols;
     s->width = width;
     s->height = height;
+    s->batch = max_pairs;
     s->cam_mode = (height == 240) ? 2u : 1u;
     s->ctf_levels = log2u(rows / 15) + 1;
     s->pyr_levels = log2u(width / cols) + s->ctf_levels;
@@ -266,6 +327,7 @@ int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_p
     carve_solver(s, nullptr, &bytes);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
+        cudaGetLastError();
         delete s;
         return set_error(PDFLOW_ERR_OOM, "arena allocation", e);
     }
@@ -285,62 +347,86 @@ int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_p
     return PDFLOW_OK;
 }
 
+int pdflow_create(unsigned rows, unsigned width, unsigned height, const pdflow_params* params, pdflow_solver** out)
+{
+    return pdflow_create_batch(rows, width, height, params, 1, out);
+}
+
 int pdflow_destroy(pdflow_solver* s)
 {
     if (!s) return PDFLOW_OK;
     cudaStreamSynchronize(s->stream);
-    for (int k = 0; k < 2; ++k)
-        if (s->solve_graph[k]) cudaGraphExecDestroy(s->solve_graph[k]);
+    for (auto& g : s->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     cudaFree(s->arena);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return PDFLOW_OK;
 }
 
-int pdflow_push_frame(pdflow_solver* s, const float* I, const float* Z)
+size_t pdflow_device_bytes(const pdflow_solver* s) { return s ? s->arena_bytes : 0; }
+
+int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float* Z)
 {
     if (!s || !I || !Z) return set_error(PDFLOW_ERR_ARG, "null argument");
-    const size_t n = size_t(s->width) * s->height;
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t b = size_t(s->width) * s->height * 4;
     s->new_slot ^= 1;  // copyNewFrames pointer swap (pdflow_cudalib.cu:203-221)
-    CUDA_TRY(cudaMemcpyAsync(s->stage_I, I, n * 4, cudaMemcpyHostToDevice, s->stream), "H2D intensity");
-    CUDA_TRY(cudaMemcpyAsync(s->stage_Z, Z, n * 4, cudaMemcpyHostToDevice, s->stream), "H2D depth");
-    CUDA_TRY(launch_pyr_level0(s->stage_I, s->stage_Z, s->height, s->width, s->pyr[s->new_slot][0], s->prm.fovh,
-                               s->stream),
+    CUDA_TRY(cudaMemcpy2DAsync(s->stage_I, s->pair_stride, I, b, b, n, cudaMemcpyHostToDevice, s->stream),
+             "H2D intensity");
+    CUDA_TRY(cudaMemcpy2DAsync(s->stage_Z, s->pair_stride, Z, b, b, n, cudaMemcpyHostToDevice, s->stream),
+             "H2D depth");
+    CUDA_TRY(launch_pyr_level0(s->stage_I, s->stage_Z, s->height, s->width, s->pyr[s->new_slot][0], s->prm.fovh, n,
+                               s->pair_stride, s->stream),
              "level-0 launch");
-    int rc = enqueue_pyramid(s, s->stream);
-    if (rc) return rc;
-    if (s->frames < 2) ++s->frames;
-    return PDFLOW_OK;
+    return push_common(s, n);
+}
+
+int pdflow_push_frame(pdflow_solver* s, const float* I, const float* Z) { return pdflow_push_frames(s, 1, I, Z); }
+
+int pdflow_push_frames_u16_device(pdflow_solver* s, unsigned n, const uint8_t* d_intensity, const uint16_t* d_depth)
+{
+    if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    s->new_slot ^= 1;
+    CUDA_TRY(launch_decode_u16(d_intensity, d_depth, s->width, s->height, s->pyr[s->new_slot][0], s->prm.fovh, n,
+                               s->pair_stride, s->stream),
+             "decode launch");
+    return push_common(s, n);
 }
 
 int pdflow_push_frame_u16_device(pdflow_solver* s, const uint8_t* d_intensity, const uint16_t* d_depth)
 {
-    if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
-    s->new_slot ^= 1;
-    CUDA_TRY(launch_decode_u16(d_intensity, d_depth, s->width, s->height, s->pyr[s->new_slot][0], s->prm.fovh,
-                               s->stream),
-             "decode launch");
-    int rc = enqueue_pyramid(s, s->stream);
-    if (rc) return rc;
-    if (s->frames < 2) ++s->frames;
-    return PDFLOW_OK;
+    return pdflow_push_frames_u16_device(s, 1, d_intensity, d_depth);
+}
+
+int pdflow_push_frames_u16(pdflow_solver* s, unsigned n, const uint8_t* intensity, const uint16_t* depth)
+{
+    if (!s || !intensity || !depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t px = size_t(s->width) * s->height * n;
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u8, intensity, px, cudaMemcpyHostToDevice, s->stream), "H2D intensity");
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u16, depth, px * 2, cudaMemcpyHostToDevice, s->stream), "H2D depth");
+    return pdflow_push_frames_u16_device(s, n, s->stage_u8, s->stage_u16);
 }
 
 int pdflow_push_frame_u16(pdflow_solver* s, const uint8_t* intensity, const uint16_t* depth)
 {
-    if (!s || !intensity || !depth) return set_error(PDFLOW_ERR_ARG, "null argument");
-    const size_t n = size_t(s->width) * s->height;
-    CUDA_TRY(cudaMemcpyAsync(s->stage_u8, intensity, n, cudaMemcpyHostToDevice, s->stream), "H2D intensity");
-    CUDA_TRY(cudaMemcpyAsync(s->stage_u16, depth, n * 2, cudaMemcpyHostToDevice, s->stream), "H2D depth");
-    return pdflow_push_frame_u16_device(s, s->stage_u8, s->stage_u16);
+    return pdflow_push_frames_u16(s, 1, intensity, depth);
 }
 
-int pdflow_solve(pdflow_solver* s)
+int pdflow_solve_batch(pdflow_solver* s, unsigned n)
 {
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     if (s->frames < 2) return set_error(PDFLOW_ERR_STATE, "solve needs two pushed frames");
-    if (!s->use_graph) return enqueue_solve(s, s->stream);
-    cudaGraphExec_t& ge = s->solve_graph[s->new_slot];
+    if (!s->use_graph) return enqueue_solve(s, s->stream, n);
+    cudaGraphExec_t ge = nullptr;
+    for (auto& g : s->graphs)
+        if (g.slot == s->new_slot && g.pairs == n && g.form == s->iter_form) {
+            ge = g.exec;
+            s->launches = g.launches;
+        }
     if (!ge) {
         cudaStream_t cap;
         CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
@@ -348,7 +434,7 @@ int pdflow_solve(pdflow_solver* s)
         cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         int rc = PDFLOW_OK;
         if (e == cudaSuccess) {
-            rc = enqueue_solve(s, cap);
+            rc = enqueue_solve(s, cap, n);
             cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
             if (e == cudaSuccess) e = e2;
         }
@@ -356,23 +442,29 @@ int pdflow_solve(pdflow_solver* s)
         if (graph) cudaGraphDestroy(graph);
         cudaStreamDestroy(cap);
         if (rc != PDFLOW_OK) return rc;
-        if (e != cudaSuccess) {
-            ge = nullptr;
-            return set_error(PDFLOW_ERR_CUDA, "solve graph capture", e);
-        }
+        if (e != cudaSuccess) return set_error(PDFLOW_ERR_CUDA, "solve graph capture", e);
+        s->graphs.push_back(pdflow_solver::GraphEntry{s->new_slot, n, s->iter_form, ge, s->launches});
     }
     CUDA_TRY(cudaGraphLaunch(ge, s->stream), "solve graph launch");
     return PDFLOW_OK;
 }
 
-int pdflow_read_flow(pdflow_solver* s, float* dx, float* dy, float* dz)
+int pdflow_solve(pdflow_solver* s) { return pdflow_solve_batch(s, 1); }
+
+int pdflow_read_flow_batch(pdflow_solver* s, unsigned n, float* dx, float* dy, float* dz)
 {
     if (!s || !dx || !dy || !dz) return set_error(PDFLOW_ERR_ARG, "null argument");
-    const size_t n = size_t(s->rows) * s->cols * 4;
-    CUDA_TRY(cudaMemcpyAsync(dx, s->dx, n, cudaMemcpyDeviceToHost, s->stream), "D2H dx");
-    CUDA_TRY(cudaMemcpyAsync(dy, s->dy, n, cudaMemcpyDeviceToHost, s->stream), "D2H dy");
-    CUDA_TRY(cudaMemcpyAsync(dz, s->dz, n, cudaMemcpyDeviceToHost, s->stream), "D2H dz");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t b = size_t(s->rows) * s->cols * 4;
+    CUDA_TRY(cudaMemcpy2DAsync(dx, b, s->dx, s->pair_stride, b, n, cudaMemcpyDeviceToHost, s->stream), "D2H dx");
+    CUDA_TRY(cudaMemcpy2DAsync(dy, b, s->dy, s->pair_stride, b, n, cudaMemcpyDeviceToHost, s->stream), "D2H dy");
+    CUDA_TRY(cudaMemcpy2DAsync(dz, b, s->dz, s->pair_stride, b, n, cudaMemcpyDeviceToHost, s->stream), "D2H dz");
     return check_status(s);
+}
+
+int pdflow_read_flow(pdflow_solver* s, float* dx, float* dy, float* dz)
+{
+    return pdflow_read_flow_batch(s, 1, dx, dy, dz);
 }
 
 int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, const float** dz)
@@ -381,6 +473,14 @@ int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, con
     if (dx) *dx = s->dx;
     if (dy) *dy = s->dy;
     if (dz) *dz = s->dz;
+    return PDFLOW_OK;
+}
+
+int pdflow_batch_info(const pdflow_solver* s, unsigned* max_pairs, size_t* pair_stride_bytes)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (max_pairs) *max_pairs = s->batch;
+    if (pair_stride_bytes) *pair_stride_bytes = s->pair_stride;
     return PDFLOW_OK;
 }
 

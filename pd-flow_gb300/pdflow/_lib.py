@@ -54,10 +54,20 @@ _SIGNATURES = {
     "pdflow_set_stream": (ctypes.c_int, [vp, vp]),
     "pdflow_get_config": (ctypes.c_int, [vp] + [ctypes.POINTER(u32)] * 5),
     "pdflow_set_graph_mode": (ctypes.c_int, [vp, ctypes.c_int]),
+    "pdflow_create_batch": (ctypes.c_int, [u32, u32, u32, ctypes.POINTER(Params), u32, ctypes.POINTER(vp)]),
+    "pdflow_push_frames": (ctypes.c_int, [vp, u32, vp, vp]),
+    "pdflow_push_frames_u16": (ctypes.c_int, [vp, u32, vp, vp]),
+    "pdflow_push_frames_u16_device": (ctypes.c_int, [vp, u32, vp, vp]),
+    "pdflow_solve_batch": (ctypes.c_int, [vp, u32]),
+    "pdflow_read_flow_batch": (ctypes.c_int, [vp, u32, vp, vp, vp]),
+    "pdflow_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(u32), ctypes.POINTER(ctypes.c_size_t)]),
+    "pdflow_device_bytes": (ctypes.c_size_t, [vp]),
     "pdflow_last_error": (ctypes.c_char_p, []),
     "pdflow_version": (ctypes.c_char_p, []),
     "pdflow_debug_solve": (ctypes.c_int, [vp, DUMP_FN, vp]),
     "pdflow_set_iteration_form": (ctypes.c_int, [vp, ctypes.c_int]),
+    "pdflow_last_solve_launches": (ctypes.c_int, [vp, ctypes.POINTER(u32)]),
+    "pdflow_time_level_iterations": (ctypes.c_int, [vp, u32, u32, u32, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_stage_median": (ctypes.c_int, [u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
 }
 
@@ -225,3 +235,62 @@ class Solver:
 
 
 PD_flow = Solver
+
+
+class BatchSolver:
+    """Many independent pairs of one configuration solved together
+    (pdflow_create_batch).  Frames are pushed as stacks [n, height, width]."""
+
+    def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
+                 use_graph: bool = True, iteration_form: int = 1):
+        lib = load()
+        self.rows, self.width, self.height, self.max_pairs = rows, width, height, max_pairs
+        self.cols = rows * 320 // 240
+        h = ctypes.c_void_p()
+        p = ctypes.byref(params) if params is not None else None
+        check(lib.pdflow_create_batch(rows, width, height, p, max_pairs, ctypes.byref(h)), "pdflow_create_batch")
+        self._h = h
+        check(lib.pdflow_set_graph_mode(h, int(use_graph)), "pdflow_set_graph_mode")
+        check(lib.pdflow_set_iteration_form(h, int(iteration_form)), "pdflow_set_iteration_form")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_bytes(self) -> int:
+        return int(load().pdflow_device_bytes(self._h))
+
+    def push_raw(self, intensity: np.ndarray, depth: np.ndarray):
+        i8 = np.ascontiguousarray(intensity, np.uint8)
+        z16 = np.ascontiguousarray(depth, np.uint16)
+        n = i8.shape[0]
+        if i8.shape != (n, self.height, self.width) or z16.shape != i8.shape:
+            raise ValueError("expected stacks [n, height, width]")
+        check(load().pdflow_push_frames_u16(self._h, n, _ptr(i8), _ptr(z16)), "pdflow_push_frames_u16")
+
+    def push_raw_device(self, n: int, d_intensity: int, d_depth: int):
+        check(load().pdflow_push_frames_u16_device(self._h, n, ctypes.c_void_p(d_intensity),
+                                                   ctypes.c_void_p(d_depth)), "pdflow_push_frames_u16_device")
+
+    def solve(self, n: int):
+        check(load().pdflow_solve_batch(self._h, n), "pdflow_solve_batch")
+
+    def read_flow(self, n: int):
+        m = self.rows * self.cols
+        out = [np.zeros((n, m), np.float32) for _ in range(3)]
+        check(load().pdflow_read_flow_batch(self._h, n, *[_ptr(a) for a in out]), "pdflow_read_flow_batch")
+        return out
+
+    def synchronize(self):
+        check(load().pdflow_synchronize(self._h), "pdflow_synchronize")
+
+    def close(self):
+        if self._h is not None:
+            load().pdflow_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,72 @@
+"""Batches: every pair of a batch equals its single-pair solve, bit for bit."""
+import numpy as np
+import pytest
+
+from pdflow import BatchSolver, Solver, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    return built_lib
+
+
+def single(rows, frames, form=1):
+    i1, z1, i2, z2 = frames
+    h, w = i1.shape
+    s = Solver(rows, w, h, iteration_form=form).initializeCUDA()
+    s.loadRGBDFrames(i1, z1, i2, z2)
+    s.solveSceneFlowGPU()
+    out = [x.copy() for x in (s.dxp, s.dyp, s.dzp)]
+    s.freeGPUMemory()
+    return out
+
+
+def batch_solve(rows, pairs, capacity=None, form=1):
+    h, w = pairs[0][0].shape
+    n = len(pairs)
+    b = BatchSolver(rows, w, h, capacity or n, iteration_form=form)
+    b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
+    b.push_raw(np.stack([p[2] for p in pairs]), np.stack([p[3] for p in pairs]))
+    b.solve(n)
+    out = b.read_flow(n)
+    b.close()
+    return out
+
+
+@pytest.mark.parametrize("vga,rows,n", [(False, 240, 4), (False, 60, 5), (True, 480, 3), (True, 240, 2)])
+def test_batch_pairs_equal_single_solves(vga, rows, n):
+    pairs = [scenes.make_pair(100 + k, vga=vga, n_objects=1 + (k % 8)) for k in range(n)]
+    got = batch_solve(rows, pairs)
+    for k, fr in enumerate(pairs):
+        ref = single(rows, fr)
+        for c in range(3):
+            assert np.array_equal(got[c][k].view(np.uint32), ref[c].view(np.uint32)), (k, c)
+
+
+def test_partial_batch_and_golden(golden_qvga):
+    """Solving n < capacity pairs; pair 0 fed the golden frames reproduces the
+    reference's CUDA output."""
+    g = golden_qvga
+    pairs = [(g["i1"], g["z1"], g["i2"], g["z2"]), scenes.make_pair(7)]
+    got = batch_solve(240, pairs, capacity=6)
+    for c, name in enumerate(("dx", "dy", "dz")):
+        assert np.array_equal(got[c][0].view(np.uint32), g[f"r240_{name}"].view(np.uint32))
+
+
+def test_batch_two_kernel_form_agrees():
+    pairs = [scenes.make_pair(200 + k) for k in range(3)]
+    a = batch_solve(120, pairs, form=1)
+    b = batch_solve(120, pairs, form=0)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_batch_rejects_bad_counts():
+    from pdflow import ERR_ARG, PDFlowError
+    b = BatchSolver(60, 320, 240, 2)
+    with pytest.raises(PDFlowError) as e:
+        b.solve(3)
+    assert e.value.code == ERR_ARG
+    b.close()
