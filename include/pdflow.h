@@ -155,6 +155,26 @@ int pdflow_batch_info(const pdflow_solver* s, unsigned* max_pairs, size_t* pair_
 /* Device memory held by the handle, in bytes (0 for NULL). */
 size_t pdflow_device_bytes(const pdflow_solver* s);
 
+/* ---- Allocation-free solve (no counterpart in the reference) ----
+ * For callers that cannot allocate device memory after start-up (a real-time
+ * or safety-critical camera loop with a fixed memory budget, or a plugin whose
+ * host framework owns every allocation): one pair solved entirely in scratch
+ * memory compiled into this library, a 12 MiB __device__ array that every GPU
+ * loading the library holds until the process exits.  It fits 320x240 frames
+ * with rows <= 120; larger configurations return PDFLOW_ERR_ARG.
+ * Inputs: both frames as device pointers, row-major uint8 intensity and
+ * uint16 depth (metres * 5000), height x width.  Outputs: device planes of
+ * rows*cols floats (column-major, as pdflow_read_flow).  Work is queued on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream) and the call
+ * returns without waiting.  The first call on a device resolves the scratch
+ * array's device address (cudaGetSymbolAddress) and sets kernel attributes:
+ * make it before any stream capture.  All calls share the scratch array, which
+ * keeps the last call's contents; calls that overlap on the GPU race on it and
+ * must be serialised by the caller.  No cudaMalloc or cudaFree is called. */
+int pdflow_solve_pair_noalloc(unsigned rows, unsigned width, unsigned height, const pdflow_params* params,
+                              const uint8_t* d_intensity1, const uint16_t* d_depth1, const uint8_t* d_intensity2,
+                              const uint16_t* d_depth2, float* d_dx, float* d_dy, float* d_dz, void* stream);
+
 /* Human-readable text of the last error on this thread. */
 const char* pdflow_last_error(void);
 

@@ -55,5 +55,6 @@ int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs);
 int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs);
 int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);
 int check_status(pdflow_solver* s);
+void set_last_error(const char* text);   // the text pdflow_last_error returns on this thread
 LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, unsigned pairs = 1);
 }  // namespace pdflow

@@ -78,6 +78,8 @@ struct Carver {
 
 namespace pdflow {
 
+void set_last_error(const char* text) { g_last_error = text; }
+
 // Waits for the handle's stream and reports (then clears) a device-side
 // timeout recorded by a bounded wait.
 int check_status(pdflow_solver* s)

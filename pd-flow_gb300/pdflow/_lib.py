@@ -62,6 +62,8 @@ _SIGNATURES = {
     "pdflow_read_flow_batch": (ctypes.c_int, [vp, u32, vp, vp, vp]),
     "pdflow_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(u32), ctypes.POINTER(ctypes.c_size_t)]),
     "pdflow_device_bytes": (ctypes.c_size_t, [vp]),
+    "pdflow_solve_pair_noalloc": (ctypes.c_int, [u32, u32, u32, ctypes.POINTER(Params), vp, vp, vp, vp, vp, vp, vp,
+                                                  vp]),
     "pdflow_last_error": (ctypes.c_char_p, []),
     "pdflow_version": (ctypes.c_char_p, []),
     "pdflow_debug_solve": (ctypes.c_int, [vp, DUMP_FN, vp]),
