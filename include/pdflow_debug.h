@@ -24,10 +24,13 @@ typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const flo
  * in CSF_cuda, pdflow_cudalib.h:71-122).  The final flow equals pdflow_solve's. */
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
-/* Selects how pdflow_solve runs a level's iterations: 1 (default) = one
- * launch per level (slab-persistent kernel), 0 = two kernels per iteration
- * (the reference's launch structure with gradient+dual and divergence+primal
- * fused).  Both give the same bits. */
+/* Selects how pdflow_solve runs a level's iterations: 2 (default) = levels
+ * above 19 200 pixels as temporally blocked shared-memory tiles (several
+ * iterations per launch), smaller levels as one launch per level; 1 = one
+ * launch per level (slab-persistent kernel; batches use two kernels per
+ * iteration for the large levels); 0 = two kernels per iteration (the
+ * reference's launch structure with gradient+dual and divergence+primal
+ * fused).  All give the same bits. */
 int pdflow_set_iteration_form(pdflow_solver* s, int form);
 
 /* Number of kernels the last pdflow_solve / pdflow_solve_batch launched

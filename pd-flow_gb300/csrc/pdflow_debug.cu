@@ -115,7 +115,7 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 
 int pdflow_set_iteration_form(pdflow_solver* s, int form)
 {
-    if (!s || (form != 0 && form != 1)) return PDFLOW_ERR_ARG;
+    if (!s || form < 0 || form > 2) return PDFLOW_ERR_ARG;
     if (s->iter_form != form) {
         cudaStreamSynchronize(s->stream);
         s->iter_form = form;   // graphs are cached per iteration form

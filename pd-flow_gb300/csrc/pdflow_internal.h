@@ -27,11 +27,12 @@ struct pdflow_solver {
     pdflow::LevelConsts L{};
     pdflow::State S{};
     float* alt[10] = {};                 // second buffer of du_acc,dv_acc,dw_acc,pd,puu,puv,pvu,pvv,pwu,pwv
+    float* alt_d[3] = {};                // second buffer of du,dv,dw (tile form)
     pdflow::LevelSol sol{};
     unsigned* flags = nullptr;           // per-CTA progress counters of the grid-form iteration
     unsigned* status = nullptr;          // device status word (0 = ok)
     int num_sms = 0;
-    int iter_form = 1;                   // 1 = one launch per level's iterations, 0 = two kernels per iteration
+    int iter_form = 2;                   // 2 = tiles for large levels, 1 = one launch per level, 0 = two kernels per iteration
     float* dx = nullptr;
     float* dy = nullptr;
     float* dz = nullptr;

@@ -40,6 +40,14 @@ IterPlan plan_iterate(LevelGeom g, int num_sms);
 unsigned iterate_smem_limit();
 // One-time function attributes (dynamic shared memory, cluster size).
 cudaError_t prepare_iterate();
+// Temporally blocked form (pdflow_tiles.cu): `kk` iterations of every tile of
+// the level, state read from `src` and the tiles' interiors written to `dst`.
+cudaError_t prepare_tiles();
+unsigned tiles_halo();
+size_t tiles_smem_bytes();
+unsigned tiles_per_level(LevelGeom g);
+cudaError_t launch_iterate_tiles(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
+                                 unsigned kk, bool last, cudaStream_t st);
 // Enqueues the level's iterations (and, in the grid form, the reset of the progress counters).
 cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st);
 

@@ -85,6 +85,7 @@ int setup_device(int dev, void** scratch, int* num_sms)
     if (e != cudaSuccess) return fail(PDFLOW_ERR_CUDA, "cudaGetDeviceProperties", e);
     if (!(prop.major == 10 && prop.minor == 3)) return fail(PDFLOW_ERR_NO_DEVICE, "needs an sm_103 (GB300) device");
     e = pdflow::prepare_iterate();
+    if (e == cudaSuccess) e = pdflow::prepare_tiles();
     if (e != cudaSuccess) return fail(PDFLOW_ERR_CUDA, "kernel attributes", e);
     void* addr = nullptr;
     e = cudaGetSymbolAddress(&addr, g_scratch);
@@ -138,7 +139,7 @@ int pdflow_solve_pair_noalloc(unsigned rows, unsigned width, unsigned height, co
     if (params) s.prm = *params;
     else pdflow_default_params(rows, &s.prm);
     s.use_graph = 0;
-    s.iter_form = 1;
+    s.iter_form = 2;
     size_t need = 0;
     pdflow::carve_solver(&s, nullptr, &need);
     if (need > kScratchBytes) {

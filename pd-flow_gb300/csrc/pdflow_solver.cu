@@ -123,6 +123,7 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     float** op[] = {&O.du, &O.dv, &O.dw, &O.pd, &O.puu, &O.puv, &O.pvu, &O.pvv, &O.pwu, &O.pwv};
     for (float** p : op) *p = cv.plane(N);
     for (float*& p : s->alt) p = cv.plane(N);
+    for (float*& p : s->alt_d) p = cv.plane(N);
     s->dx = cv.plane(N);
     s->dy = cv.plane(N);
     s->dz = cv.plane(N);
@@ -172,9 +173,26 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
     Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
     *fin = s->S;
     const IterPlan pl = plan_iterate(g, s->num_sms);
-    const bool one_launch = s->iter_form == 1 && iters > 0 && (pairs == 1 || pl.mode != kIterGrid) &&
+    const bool tiles = s->iter_form == 2 && iters > 0 && pl.mode == kIterGrid && pairs > 1;
+    const bool one_launch = s->iter_form >= 1 && iters > 0 && !tiles && (pairs == 1 || pl.mode != kIterGrid) &&
                             pl.smem_bytes <= iterate_smem_limit();
-    if (one_launch) {
+    if (tiles) {
+        State cur = s->S;
+        State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
+                  s->alt[5], s->alt[6], s->alt[7], s->alt[8], s->alt[9]};
+        const unsigned h = tiles_halo();
+        for (unsigned done = 0; done < iters;) {
+            const unsigned kk = (iters - done < h) ? iters - done : h;
+            CUDA_TRY(launch_iterate_tiles(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st),
+                     "tile iteration launch");
+            const State t = cur;
+            cur = nxt;
+            nxt = t;
+            done += kk;
+            *count += 1;
+        }
+        *fin = cur;
+    } else if (one_launch) {
         IterArgs a{};
         a.g = g;
         a.L = s->L;
@@ -306,6 +324,7 @@ int pdflow_create_batch(unsigned rows, unsigned width, unsigned height, const pd
         static bool prepared = false;
         if (!prepared) {
             CUDA_TRY(prepare_iterate(), "kernel attributes");
+            CUDA_TRY(prepare_tiles(), "kernel attributes");
             prepared = true;
         }
     }

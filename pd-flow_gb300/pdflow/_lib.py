@@ -131,7 +131,7 @@ class Solver:
     freeGPUMemory."""
 
     def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 1):
+                 use_graph: bool = True, iteration_form: int = 2):
         self.rows, self.width, self.height = rows, width, height
         self.cols = rows * 320 // 240
         self.params = params
@@ -244,7 +244,7 @@ class BatchSolver:
     (pdflow_create_batch).  Frames are pushed as stacks [n, height, width]."""
 
     def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 1):
+                 use_graph: bool = True, iteration_form: int = 2):
         lib = load()
         self.rows, self.width, self.height, self.max_pairs = rows, width, height, max_pairs
         self.cols = rows * 320 // 240

@@ -55,12 +55,14 @@ def test_partial_batch_and_golden(golden_qvga):
         assert np.array_equal(got[c][0].view(np.uint32), g[f"r240_{name}"].view(np.uint32))
 
 
-def test_batch_two_kernel_form_agrees():
-    pairs = [scenes.make_pair(200 + k) for k in range(3)]
-    a = batch_solve(120, pairs, form=1)
-    b = batch_solve(120, pairs, form=0)
-    for x, y in zip(a, b):
-        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+@pytest.mark.parametrize("vga,rows", [(False, 120), (False, 240), (True, 480)])
+def test_batch_iteration_forms_agree(vga, rows):
+    pairs = [scenes.make_pair(200 + k, vga=vga) for k in range(3)]
+    a = batch_solve(rows, pairs, form=2)
+    for form in (1, 0):
+        b = batch_solve(rows, pairs, form=form)
+        for x, y in zip(a, b):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), form
 
 
 def test_batch_rejects_bad_counts():
