@@ -185,13 +185,16 @@ def measured_peaks():
 
 
 def profiled_traffic():
-    """Per-iteration DRAM bytes of the finest level's iteration kernels from a
-    committed ncu summary (profiles/roofline_traffic.json), else None."""
+    """DRAM bytes per pixel-iteration of the tile iteration kernel, from the
+    committed ncu summary (the `bytes_per_px_iter:` line), else None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
-            return json.load(f)
+        with open(os.path.join(ROOT, "profiles", "k_iterate_tiles_vga_batch16.md")) as f:
+            for line in f:
+                if line.startswith("bytes_per_px_iter:"):
+                    return {"bytes_per_px_iter": float(line.split(":")[1])}
     except (OSError, ValueError):
-        return None
+        pass
+    return None
 
 
 def ours(args):
@@ -262,15 +265,18 @@ def ours(args):
     with torch.cuda.stream(stream):
         _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
         _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
-    alg_bytes = ALG_BYTES_PER_PX_ITER * B * R_f * C_f          # per iteration (one dual + one primal launch)
+    alg_bytes = ALG_BYTES_PER_PX_ITER * B * R_f * C_f          # per iteration
     achieved = alg_bytes / (ms.value / iters / 1000.0) / 1e9
     trf = profiled_traffic()
     traffic = None
-    if trf and trf.get("rows") == ROWS and trf.get("bytes_per_px_iter"):
+    if trf and trf.get("bytes_per_px_iter"):
+        # DRAM bytes per iteration, scaled from a 16-pair capture at 240x320
+        # (traffic per pixel-iteration does not depend on the batch size)
         traffic = float(trf["bytes_per_px_iter"]) * B * R_f * C_f
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": f"finest-level iteration (480x640, {B} pairs; dual+primal per iteration)",
+                "traffic": traffic, "traffic_basis": "DRAM bytes per iteration of the timed level (scaled ncu capture)",
+                "peak_kind": peak_kind,
+                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles, <=4 iterations per launch)",
                 "algorithmic_bytes_per_px_iter": ALG_BYTES_PER_PX_ITER,
                 "ms_per_iteration": ms.value / iters}
 

@@ -155,6 +155,38 @@ int pdflow_batch_info(const pdflow_solver* s, unsigned* max_pairs, size_t* pair_
 /* Device memory held by the handle, in bytes (0 for NULL). */
 size_t pdflow_device_bytes(const pdflow_solver* s);
 
+/* ---- Slot-addressed batches (serving; no counterpart in the reference) ----
+ * Each of the handle's max_pairs slots is an independent camera stream: a
+ * push moves the slot's newest frame (pyramid kept on the device) to the
+ * previous-frame position and decodes the new one into its place, so a
+ * stream's frame t is decoded once and reused as frame t-1 of the next pair.
+ * slots[k] (distinct, < max_pairs) is the slot of input k; inputs are
+ * [n][height][width].  Once a handle has been pushed per slot it accepts only
+ * slot calls (and vice versa: PDFLOW_ERR_STATE). */
+int pdflow_push_frames_slots_u16(pdflow_solver* s, unsigned n, const unsigned* slots, const uint8_t* intensity,
+                                 const uint16_t* depth);
+int pdflow_push_frames_slots_u16_device(pdflow_solver* s, unsigned n, const unsigned* slots,
+                                        const uint8_t* d_intensity, const uint16_t* d_depth);
+/* Solves the listed slots (each must hold two frames) in one batch. */
+int pdflow_solve_slots(pdflow_solver* s, unsigned n, const unsigned* slots);
+/* Copies the listed slots' motion fields to host arrays [n][rows*cols]. */
+int pdflow_read_flow_slots(pdflow_solver* s, unsigned n, const unsigned* slots, float* dx, float* dy, float* dz);
+
+/* ---- Energy of a solution (no counterpart in the reference) ----
+ * The functional the iterations minimise, evaluated at the last solve's
+ * finest-level solution of pairs [0, n) (blocks; host array [n]):
+ *   sum over pixels of |I2(x+u) - I1(x)| + mu(x) |Z2(x+u) - Z1(x) - dw|
+ *   + lambda_i (|r grad du| + |r grad dv|) + lambda_d |r grad dw|
+ * with the warped data terms and the data weight mu(x) of the solver's own
+ * warping at the solution's flow (pdflow_cudalib.cu:629-808) and the
+ * ri/rj-weighted forward differences of its gradient (:982-1013). */
+int pdflow_energy_batch(pdflow_solver* s, unsigned n, float* energies);
+
+/* Device planes of pair 0's finest-level image-plane solution (du, dv in
+ * pixels of the finest solved level, dw in metres; column-major rows*cols;
+ * pair k at + k * pair_stride_bytes), valid after a solve completes. */
+int pdflow_image_flow_device(pdflow_solver* s, const float** du, const float** dv, const float** dw);
+
 /* ---- Allocation-free solve (no counterpart in the reference) ----
  * For callers that cannot allocate device memory after start-up (a real-time
  * or safety-critical camera loop with a fixed memory budget, or a plugin whose

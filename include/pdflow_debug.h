@@ -52,6 +52,17 @@ int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const fl
                         const float* dv, const float* dw, float* du_l, float* dv_l, float* dw_l, int32_t* sel,
                         void* stream);
 
+/* Runs levels [first, last] of the coarse-to-fine schedule for pairs [0, n)
+ * (no graph, on the handle's stream, blocking).  `d_seed` (device,
+ * [n][3][N_first] floats: du, dv in level pixels, dw in metres; may be NULL)
+ * replaces level `first`'s upsampled start, with zero duals; every solved
+ * level runs ceil(num_max_iter * iter_scale) iterations.  With energy_level in
+ * [first, last], energies[n] (host) receives that level's solution energy
+ * (the functional of pdflow_energy_batch).  first = 0, last >= the finest
+ * level, no seed, scale 1 is pdflow_solve_batch. */
+int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned last, const float* d_seed,
+                        float iter_scale, int energy_level, float* energies);
+
 #ifdef __cplusplus
 }
 #endif

@@ -139,3 +139,49 @@ def decode_frame(intensity: np.ndarray, depth: np.ndarray):
     f(ctypes.c_uint(w), ctypes.c_uint(h), _ptr(np.ascontiguousarray(intensity, np.uint8)),
       _ptr(np.ascontiguousarray(depth, np.uint16)), _ptr(I), _ptr(Z))
     return I, Z
+
+
+def energy(R: int, C: int, old: tuple, new: tuple, du, dv, dw, mu: float = 75.0, lambda_i: float = 0.04,
+           lambda_d: float = 0.35, precision: str = "f64") -> float:
+    """Energy of a level solution (or_energy, pdflow_oracle.c): `old`/`new` are
+    the two frames' level images (colour, depth, xx, yy), column-major R*C;
+    du, dv the total image-plane flow in level pixels, dw in metres."""
+    dt = np.float64 if precision == "f64" else np.float32
+    cv = lambda a: np.ascontiguousarray(np.asarray(a, dtype=dt).ravel())
+    o = [cv(a) for a in old]
+    n = [cv(a) for a in new]
+    u, v, w = cv(du), cv(dv), cv(dw)
+    f = _stage("energy", precision)
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    f.restype = ctypes.c_double
+    keep = [_ptr_array([o[k], n[k]]) for k in range(4)]
+    return float(f(ctypes.c_uint(R), ctypes.c_uint(C), real(mu), real(lambda_i), real(lambda_d),
+                   *[ctypes.cast(p, ctypes.c_void_p) for p in keep], _ptr(u), _ptr(v), _ptr(w)))
+
+
+def solve_seeded(rows: int, width: int, height: int, I1, Z1, I2, Z2, first: int, seed, iter_scale: float = 1.0,
+                 precision: str = "f64", dump: bool = False):
+    """The solve started at level `first` from `seed` ([3][N_first]: du, dv in
+    level pixels, dw in metres) with zero duals, every solved level running
+    ceil(num_max_iter * iter_scale) iterations (iter_scale is rounded to
+    float32 first, as the GPU library receives it)."""
+    L = lib()
+    cols = rows * 320 // 240
+    n = rows * cols
+    dx, dy, dz = (np.zeros(n, np.float32) for _ in range(3))
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (I1, Z1, I2, Z2)]
+    sd = np.ascontiguousarray(np.asarray(seed, dtype=np.float32).ravel())
+    store = {}
+    dt = np.float64 if precision == "f64" else np.float32
+
+    def _cb(ctx, name, level, ptr, cnt):
+        store[(name.decode(), level)] = np.ctypeslib.as_array(ptr, shape=(cnt,)).astype(dt).copy()
+
+    cb = DUMP_FN[precision](_cb) if dump else ctypes.cast(None, DUMP_FN[precision])
+    f = getattr(L, f"or_solve_seeded_{precision}")
+    f.argtypes = [ctypes.c_uint] * 3 + [_f32p] * 4 + [ctypes.c_uint, _f32p, ctypes.c_double] + [_f32p] * 3 + \
+                 [DUMP_FN[precision], ctypes.c_void_p]
+    rc = f(rows, width, height, *arrs, first, sd, float(np.float32(iter_scale)), dx, dy, dz, cb, None)
+    if rc != 0:
+        raise ValueError(f"oracle rejected the seeded solve (rows={rows}, first={first})")
+    return (dx, dy, dz, store) if dump else (dx, dy, dz)

@@ -617,6 +617,49 @@ void SFX(or_motion_field)(long N, unsigned cols, real fovh, const real* d_old,
 }
 
 /* ------------------------------------------------------------------------- */
+/* Energy of a level solution (du, dv total image-plane flow in level pixels, */
+/* dw in metres): the data and TV terms the iterations minimise, with the     */
+/* warped residuals and data weight of the solver's own set-up at that flow:  */
+/* Rij (:725-779), image gradients (:574-627), warping (:629-721), computeMu  */
+/* (:781-784); forward differences as computeGradient (:982-1013).  The       */
+/* reference has no energy; the GPU library's pdflow_energy_batch evaluates   */
+/* the same functional.  Level images: [0] = old frame, [1] = new frame.      */
+/* ------------------------------------------------------------------------- */
+static real* or_alloc(size_t n);
+
+double SFX(or_energy)(unsigned R, unsigned C, real mu_p, real li, real ld,
+                      const real* const col[2], const real* const dep[2],
+                      const real* const xx[2], const real* const yy[2],
+                      const real* du, const real* dv, const real* dw)
+{
+    const long N = (long)R * C;
+    real* w[14];
+    for (int q = 0; q < 14; ++q) w[q] = or_alloc((size_t)N);
+    real *ri = w[0], *rj = w[1], *ri2 = w[2], *rj2 = w[3], *dcu_a = w[4], *dcv_a = w[5], *ddu_a = w[6],
+         *ddv_a = w[7], *dct = w[8], *dcu = w[9], *dcv = w[10], *ddt = w[11], *ddu = w[12], *ddv = w[13];
+    SFX(or_rij)(R, C, xx[0], yy[0], dep[0], xx[1], yy[1], dep[1], ri, rj, ri2, rj2);
+    SFX(or_im_gradients)(R, C, col[1], dep[1], ri2, rj2, dcu_a, dcv_a, ddu_a, ddv_a);
+    SFX(or_warping)(R, C, col[1], col[0], dep[1], dep[0], dcu_a, dcv_a, ddu_a, ddv_a, du, dv,
+                    dct, dcu, dcv, ddt, ddu, ddv);
+    double e = 0.0;
+    for (long i = 0; i < N; ++i) {
+        const unsigned v = (unsigned)(i % R), u = (unsigned)(i / R);
+        const int lu = (u == C - 1), lv = (v == R - 1);
+        const real m = mu_p / (K(1.0) + K(1000.0) * (ddu[i] * ddu[i] + ddv[i] * ddv[i] + ddt[i] * ddt[i]));
+        const double gu1 = lu ? 0.0 : (double)(ri[i] * (du[i + R] - du[i]));
+        const double gu2 = lv ? 0.0 : (double)(rj[i] * (du[i + 1] - du[i]));
+        const double gv1 = lu ? 0.0 : (double)(ri[i] * (dv[i + R] - dv[i]));
+        const double gv2 = lv ? 0.0 : (double)(rj[i] * (dv[i + 1] - dv[i]));
+        const double gw1 = lu ? 0.0 : (double)(ri[i] * (dw[i + R] - dw[i]));
+        const double gw2 = lv ? 0.0 : (double)(rj[i] * (dw[i + 1] - dw[i]));
+        e += fabs((double)dct[i]) + (double)m * fabs((double)ddt[i] - (double)dw[i]);
+        e += (double)li * (hypot(gu1, gu2) + hypot(gv1, gv2)) + (double)ld * hypot(gw1, gw2);
+    }
+    for (int q = 0; q < 14; ++q) free(w[q]);
+    return e;
+}
+
+/* ------------------------------------------------------------------------- */
 /* Whole solve: PD_flow_opencv::createImagePyramidGPU (scene_flow_impair.cpp: */
 /* 80-93) for two frames, then solveSceneFlowGPU (:95-168).                   */
 /* Inputs are float column-major (R_img = height rows), the staging buffers  */
@@ -627,11 +670,16 @@ typedef void (*or_dump_fn)(void* ctx, const char* name, int level, const real* d
 
 static real* or_alloc(size_t n) { return (real*)calloc(n ? n : 1, sizeof(real)); }
 
-int SFX(or_solve)(unsigned rows, unsigned width, unsigned height,
-                  const float* I1, const float* Z1, const float* I2, const float* Z2,
-                  const unsigned* iters_override,
-                  float* dx_out, float* dy_out, float* dz_out,
-                  or_dump_fn dump, void* ctx)
+/* `first` > 0 starts at that level from `seed` ([3][N_first] floats: du, dv
+ * in level pixels, dw in metres) instead of the upsampled coarser solution,
+ * with zero duals (the GPU library's warm start); every solved level then
+ * runs ceil(num_max_iter * iter_scale) iterations when iter_scale < 1. */
+static int SFX(or_solve_impl)(unsigned rows, unsigned width, unsigned height,
+                              const float* I1, const float* Z1, const float* I2, const float* Z2,
+                              const unsigned* iters_override,
+                              float* dx_out, float* dy_out, float* dz_out,
+                              or_dump_fn dump, void* ctx,
+                              unsigned first, const float* seed, double iter_scale)
 {
     or_cfg c;
     if (or_make_cfg(&c, rows, width, height, iters_override) != 0) return -1;
@@ -678,7 +726,7 @@ int SFX(or_solve)(unsigned rows, unsigned width, unsigned height,
     real* dx = or_alloc(Nmax); real* dy = or_alloc(Nmax); real* dz = or_alloc(Nmax);
     const unsigned lw = or_log2u(width / c.cols);
 
-    for (unsigned i = 0; i < c.ctf_levels; ++i) {
+    for (unsigned i = first; i < c.ctf_levels; ++i) {
         const unsigned sdiv = 1u << (c.ctf_levels - (i + 1));
         const unsigned Ci = c.cols / sdiv, Ri = c.rows / sdiv;
         const unsigned li = c.ctf_levels - i + lw - 1;    /* level_image, :108 */
@@ -687,7 +735,14 @@ int SFX(or_solve)(unsigned rows, unsigned width, unsigned height,
         for (int q = 0; q < S_N; ++q) memset(s[q], 0, sizeof(real) * (size_t)N);
         memset(L[L_DUP], 0, sizeof(real) * (size_t)N);
         memset(L[L_DVP], 0, sizeof(real) * (size_t)N);
-        if (i > 0) {
+        if (i == first && seed) {
+            for (long k = 0; k < N; ++k) {
+                L[L_DUP][k] = (real)seed[k];
+                L[L_DVP][k] = (real)seed[N + k];
+                s[S_DW][k] = (real)seed[2 * N + k];
+                s[S_DWA][k] = (real)seed[2 * N + k];
+            }
+        } else if (i > 0) {
             const real* lc[10];
             for (int q = 0; q < 10; ++q) lc[q] = lsol[q];
             real* out8[8] = {s[S_DW], s[S_PD], s[S_PUU], s[S_PUV], s[S_PVU], s[S_PVV], s[S_PWU], s[S_PWV]};
@@ -715,7 +770,9 @@ int SFX(or_solve)(unsigned rows, unsigned width, unsigned height,
         }
         const real* Lc[L_N];
         for (int q = 0; q < L_N; ++q) Lc[q] = L[q];
-        for (unsigned it = 0; it < c.num_max_iter[i]; ++it) {
+        unsigned iters = c.num_max_iter[i];
+        if (iter_scale < 1.0) iters = (unsigned)ceil((double)iters * iter_scale);
+        for (unsigned it = 0; it < iters; ++it) {
             SFX(or_dual_step)(Ri, Ci, c.lambda_i, c.lambda_d, s, Lc, gr);
             SFX(or_primal_step)(Ri, Ci, c.lambda_i, c.lambda_d, s, Lc, dv3);
         }
@@ -756,6 +813,27 @@ int SFX(or_solve)(unsigned rows, unsigned width, unsigned height,
 
 /* Configuration query for tests: fills ctf_levels, pyr_levels, cols, cam_mode
  * and the 6-entry iteration schedule. */
+int SFX(or_solve)(unsigned rows, unsigned width, unsigned height,
+                  const float* I1, const float* Z1, const float* I2, const float* Z2,
+                  const unsigned* iters_override,
+                  float* dx_out, float* dy_out, float* dz_out,
+                  or_dump_fn dump, void* ctx)
+{
+    return SFX(or_solve_impl)(rows, width, height, I1, Z1, I2, Z2, iters_override, dx_out, dy_out, dz_out, dump,
+                              ctx, 0, 0, 1.0);
+}
+
+int SFX(or_solve_seeded)(unsigned rows, unsigned width, unsigned height,
+                         const float* I1, const float* Z1, const float* I2, const float* Z2,
+                         unsigned first, const float* seed, double iter_scale,
+                         float* dx_out, float* dy_out, float* dz_out,
+                         or_dump_fn dump, void* ctx)
+{
+    if (!seed || first == 0) return -1;
+    return SFX(or_solve_impl)(rows, width, height, I1, Z1, I2, Z2, 0, dx_out, dy_out, dz_out, dump, ctx, first,
+                              seed, iter_scale);
+}
+
 int SFX(or_config)(unsigned rows, unsigned width, unsigned height, unsigned* out10)
 {
     or_cfg c;

@@ -15,12 +15,9 @@ using namespace pdflow;
 
 namespace {
 
-int fail(const char* what, cudaError_t e)
-{
-    // Report through the solver's error slot by a failing no-op query.
-    std::fprintf(stderr, "pdflow debug: %s: %s\n", what, cudaGetErrorString(e));
-    return PDFLOW_ERR_CUDA;
-}
+int fail(const char* what, cudaError_t e) { return set_error_code(PDFLOW_ERR_CUDA, what, e); }
+
+int fail(int code, const char* what) { return set_error_code(code, what); }
 
 struct Dumper {
     pdflow_dump_fn fn;
@@ -172,6 +169,31 @@ int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const fl
     cudaError_t e = launch_median(g, false, o, L, S, out, nullptr, nullptr, nullptr, p, sel, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     return e == cudaSuccess ? PDFLOW_OK : fail("stage median", e);
+}
+
+int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned last, const float* d_seed,
+                        float iter_scale, int energy_level, float* energies)
+{
+    if (!s) return fail(PDFLOW_ERR_ARG, "null handle");
+    if (n == 0 || n > s->batch) return fail(PDFLOW_ERR_ARG, "pair count out of range");
+    if (first >= s->ctf_levels || last < first) return fail(PDFLOW_ERR_ARG, "level range out of range");
+    if (s->frames < 2) return fail(PDFLOW_ERR_STATE, "solve needs two pushed frames");
+    if (!(iter_scale > 0.f)) return fail(PDFLOW_ERR_ARG, "iteration scale must be positive");
+    if (first > 0 && !d_seed) return fail(PDFLOW_ERR_ARG, "a level after the coarsest starts from a seed");
+    pdflow::SolvePlan plan;
+    plan.first = first;
+    plan.last = last;
+    plan.seed = d_seed;
+    plan.iter_scale = iter_scale;
+    plan.energy_level = energy_level;
+    plan.energy = energy_level >= 0 ? s->energy : nullptr;
+    int rc = pdflow::enqueue_solve(s, s->stream, n, plan);
+    if (rc) return rc;
+    if (plan.energy && energies) {
+        cudaError_t e = cudaMemcpyAsync(energies, s->energy, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream);
+        if (e != cudaSuccess) return fail(PDFLOW_ERR_CUDA, "D2H energies");
+    }
+    return pdflow::check_status(s);
 }
 
 }  // extern "C"

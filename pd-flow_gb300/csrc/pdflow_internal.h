@@ -40,10 +40,16 @@ struct pdflow_solver {
     unsigned batch = 1;                  // pairs the arena holds
     size_t pair_stride = 0;              // bytes between pair k and pair k+1 buffers
     unsigned launches = 0;               // kernel launches of the last enqueued solve
+    unsigned* map = nullptr;             // device [batch]: arena slots of a slot-addressed push / solve
+    float* energy = nullptr;             // device [2 * batch]: energies written by a solve
+    float* seed = nullptr;               // device [batch][3][seed level N]: warm-start fields
+    int slot_mode = 0;                   // 1 once frames were pushed per slot (then only per slot)
+    std::vector<unsigned char> slot_frames;   // frames pushed per slot (saturates at 2)
     struct GraphEntry {
         int slot;
         unsigned pairs;
         int form;
+        unsigned kind;                   // which enqueue sequence (plain, slot-mapped, learned ...)
         cudaGraphExec_t exec;
         unsigned launches;
     };
@@ -51,9 +57,34 @@ struct pdflow_solver {
 };
 
 namespace pdflow {
+
+// Which part of the coarse-to-fine schedule an enqueue runs, and how.
+struct SolvePlan {
+    unsigned first = 0;                  // first level solved
+    unsigned last = ~0u;                 // last level solved (clamped to the finest)
+    const float* seed = nullptr;         // device [pairs][3][N_first]: level `first` starts from it
+    float iter_scale = 1.f;              // iterations of every solved level: ceil(num_max_iter * scale)
+    int energy_level = -1;               // after this level's median, its energy goes to ...
+    float* energy = nullptr;             // ... device [pairs]
+    const unsigned* map = nullptr;       // device [pairs] arena slots (null: slots 0..pairs-1)
+};
+
+constexpr unsigned kSeedLevel = 2;       // the 60x80 level (15x20 -> 30x40 -> 60x80)
+constexpr unsigned kSeedN = 60 * 80;
+
 void carve_solver(pdflow_solver* s, char* base, size_t* used);
-int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs);
-int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs);
+int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs, const unsigned* map = nullptr);
+int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const SolvePlan& plan = SolvePlan());
+int enqueue_energy(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, float* out,
+                   const unsigned* map = nullptr);
+unsigned scaled_iters(unsigned iters, float scale);
+// Runs fn(s, stream, pairs, ctx) on the handle's stream, through a cached CUDA
+// graph keyed by (new frame slot, pairs, iteration form, kind) in graph mode.
+// Whatever fn reads from ctx is baked into the graph: equal kinds must mean
+// equal ctx contents.
+using EnqueueFn = int (*)(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void* ctx);
+int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx);
+int set_error_code(int code, const char* what, cudaError_t e = cudaSuccess);
 int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);
 int check_status(pdflow_solver* s);
 void set_last_error(const char* text);   // the text pdflow_last_error returns on this thread

@@ -79,9 +79,9 @@ template <int kMode>
 __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
 {
     extern __shared__ float sm[];
-    if (kMode != kIterGrid && blockIdx.y > 0) {
-        // batch: pair blockIdx.y of a strided arena
-        const size_t po = (size_t)blockIdx.y * a.g.pstride;
+    if (a.g.map || (kMode != kIterGrid && blockIdx.y > 0)) {
+        // batch: the pair of grid row y (the grid form solves one pair) of a strided arena
+        const size_t po = pair_off(a.g.map, a.g.pstride, kMode == kIterGrid ? 0u : blockIdx.y);
         a.L = at(a.L, po);
         a.du = at(a.du, po);
         a.dv = at(a.dv, po);

@@ -33,11 +33,12 @@ __device__ __forceinline__ void write_xy(PyrLevel out, unsigned R, unsigned C, u
 // transpose through a 32x33 shared tile so that both sides are coalesced).
 __global__ void __launch_bounds__(1024) k_decode_u16(const uint8_t* __restrict__ img,
                                                      const uint16_t* __restrict__ depth, unsigned W, unsigned H,
-                                                     PyrLevel out, float fovh, size_t pstride)
+                                                     PyrLevel out, float fovh, size_t pstride,
+                                                     const unsigned* __restrict__ map)
 {
     img += (size_t)blockIdx.z * W * H;
     depth += (size_t)blockIdx.z * W * H;
-    out = at(out, (size_t)blockIdx.z * pstride);
+    out = at(out, pair_off(map, pstride, blockIdx.z));
     __shared__ float sc[32][33];
     __shared__ float sz[32][33];
     const unsigned x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
@@ -61,9 +62,9 @@ __global__ void __launch_bounds__(1024) k_decode_u16(const uint8_t* __restrict__
 }
 
 __global__ void k_pyr_level0(const float* __restrict__ I, const float* __restrict__ Z, unsigned R, unsigned C,
-                             PyrLevel out, float fovh, size_t pstride)
+                             PyrLevel out, float fovh, size_t pstride, const unsigned* __restrict__ map)
 {
-    const size_t po = (size_t)blockIdx.y * pstride;
+    const size_t po = pair_off(map, pstride, blockIdx.y);
     I = at(I, po);
     Z = at(Z, po);
     out = at(out, po);
@@ -76,9 +77,10 @@ __global__ void k_pyr_level0(const float* __restrict__ I, const float* __restric
     write_xy(out, R, C, v, u, idx, z, fovh);
 }
 
-__global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, size_t pstride)
+__global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, size_t pstride,
+                           const unsigned* __restrict__ map)
 {
-    const size_t po = (size_t)blockIdx.y * pstride;
+    const size_t po = pair_off(map, pstride, blockIdx.y);
     prev = at(prev, po);
     out = at(out, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,9 +146,10 @@ __global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, 
 // assignZeros + upsampleCopy/upsampleFilterPrevSolution (pdflow_cudalib.cu:
 // 439-569) as a gather over the coarse solution (the zero-inserted taps
 // contribute exactly zero and are skipped), followed by computeRij (:725-779).
-__global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S)
+__global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S,
+                             const float* __restrict__ seed)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     cs = at(cs, po);
     o = at(o, po);
     n = at(n, po);
@@ -158,7 +161,12 @@ __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, P
     const unsigned v = index % R, u = index / R;
 
     float du = 0.f, dv = 0.f, dw = 0.f, pd = 0.f, puu = 0.f, puv = 0.f, pvu = 0.f, pvv = 0.f, pwu = 0.f, pwv = 0.f;
-    if (!first) {
+    if (seed) {   // warm start: a predicted solution of this level, duals from zero
+        const float* sp = seed + (size_t)blockIdx.y * 3 * g.N;
+        du = sp[index];
+        dv = sp[g.N + index];
+        dw = sp[2 * g.N + index];
+    } else if (!first) {
         const unsigned Rc = R / 2;
         const bool inner = (v > 1) && (v < R - 2) && (u > 1) && (u < C - 2);
         float acu_weight = 1.f;
@@ -238,7 +246,7 @@ __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, P
 // computeImGradients (pdflow_cudalib.cu:574-627) on the new frame.
 __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     n = at(n, po);
     L = at(L, po);
     const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
@@ -276,7 +284,7 @@ __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 // performWarping (pdflow_cudalib.cu:629-652) + computeMu/computeStepSizes (:781-808).
 __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     o = at(o, po);
     n = at(n, po);
     L = at(L, po);
@@ -319,7 +327,7 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
 // ---------------------------------------------------------------------------
 __global__ void k_dual(LevelGeom g, LevelConsts L, State S, Params p)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     L = at(L, po);
     S = at(S, po);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -344,7 +352,7 @@ __global__ void k_dual(LevelGeom g, LevelConsts L, State S, Params p)
 
 __global__ void k_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     L = at(L, po);
     S = at(S, po);
     depth_old = at(depth_old, po);
@@ -376,7 +384,7 @@ __global__ void k_primal(LevelGeom g, LevelConsts L, State S, Params p, bool las
 // saturateVariables alone, for a level scheduled with zero iterations.
 __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     L = at(L, po);
     S = at(S, po);
     depth_old = at(depth_old, po);
@@ -451,7 +459,7 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
 __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, LevelSol out, float* dx,
                          float* dy, float* dz, Params p, int32_t* sel)
 {
-    const size_t po = (size_t)blockIdx.y * g.pstride;
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     o = at(o, po);
     L = at(L, po);
     S = at(S, po);
@@ -524,39 +532,113 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     }
 }
 
+// Frame t's pyramid level becomes frame t-1's, for the mapped slots (float4
+// copies; level planes are 16-byte aligned and padded to whole float4s).
+__global__ void k_pyr_copy(PyrLevel src, PyrLevel dst, unsigned n, size_t pstride, const unsigned* __restrict__ map)
+{
+    const size_t po = pair_off(map, pstride, blockIdx.y);
+    src = at(src, po);
+    dst = at(dst, po);
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (4 * i >= n) return;
+    if (4 * i + 4 <= n) {
+        reinterpret_cast<float4*>(dst.col)[i] = reinterpret_cast<const float4*>(src.col)[i];
+        reinterpret_cast<float4*>(dst.dep)[i] = reinterpret_cast<const float4*>(src.dep)[i];
+        reinterpret_cast<float4*>(dst.xx)[i] = reinterpret_cast<const float4*>(src.xx)[i];
+        reinterpret_cast<float4*>(dst.yy)[i] = reinterpret_cast<const float4*>(src.yy)[i];
+    } else {
+        for (unsigned k = 4 * i; k < n; ++k) {
+            dst.col[k] = src.col[k];
+            dst.dep[k] = src.dep[k];
+            dst.xx[k] = src.xx[k];
+            dst.yy[k] = src.yy[k];
+        }
+    }
+}
+
+// The warp point of the energy: the solution's total image-plane flow.
+__global__ void k_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L)
+{
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    at(L.du_prev, po)[i] = at(sol.du, po)[i];
+    at(L.dv_prev, po)[i] = at(sol.dv, po)[i];
+}
+
+// One CTA per pair; fixed thread-to-pixel assignment and a fixed reduction
+// tree, so the sum is deterministic.  With du = dv = 0 increments at the warp
+// point the linearised data terms equal the warped residuals.
+__global__ void __launch_bounds__(1024) k_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p,
+                                                 float* __restrict__ energies)
+{
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
+    sol = at(sol, po);
+    L = at(L, po);
+    const unsigned R = g.R, C = g.C;
+    double acc = 0.0;
+    for (unsigned i = threadIdx.x; i < g.N; i += blockDim.x) {
+        const unsigned v = i % R, u = i / R;
+        const float U = sol.du[i], V = sol.dv[i], W = sol.dw[i], ri = L.ri[i], rj = L.rj[i];
+        const bool lu = u == C - 1, lv = v == R - 1;
+        const float gu1 = lu ? 0.f : mul(ri, sub(sol.du[i + R], U)), gu2 = lv ? 0.f : mul(rj, sub(sol.du[i + 1], U));
+        const float gv1 = lu ? 0.f : mul(ri, sub(sol.dv[i + R], V)), gv2 = lv ? 0.f : mul(rj, sub(sol.dv[i + 1], V));
+        const float gw1 = lu ? 0.f : mul(ri, sub(sol.dw[i + R], W)), gw2 = lv ? 0.f : mul(rj, sub(sol.dw[i + 1], W));
+        double e = fabs((double)L.dct[i]) + (double)L.mu[i] * fabs((double)L.ddt[i] - (double)W);
+        e += (double)p.lambda_i * (hypot((double)gu1, (double)gu2) + hypot((double)gv1, (double)gv2));
+        e += (double)p.lambda_d * hypot((double)gw1, (double)gw2);
+        acc += e;
+    }
+    __shared__ double red[1024];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (unsigned w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) energies[blockIdx.y] = (float)red[0];
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
-                              float fovh, unsigned pairs, size_t pstride, cudaStream_t st)
+                              float fovh, unsigned pairs, size_t pstride, cudaStream_t st, const unsigned* map)
 {
     dim3 grid((W + 31) / 32, (H + 31) / 32, pairs), block(32, 32);
-    k_decode_u16<<<grid, block, 0, st>>>(img, depth, W, H, out, fovh, pstride);
+    k_decode_u16<<<grid, block, 0, st>>>(img, depth, W, H, out, fovh, pstride, map);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pyr_level0(const float* I, const float* Z, unsigned R, unsigned C, PyrLevel out, float fovh,
-                              unsigned pairs, size_t pstride, cudaStream_t st)
+                              unsigned pairs, size_t pstride, cudaStream_t st, const unsigned* map)
 {
-    k_pyr_level0<<<dim3(blocks_for(R * C), pairs), kBlock, 0, st>>>(I, Z, R, C, out, fovh, pstride);
+    k_pyr_level0<<<dim3(blocks_for(R * C), pairs), kBlock, 0, st>>>(I, Z, R, C, out, fovh, pstride, map);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, unsigned pairs,
-                            size_t pstride, cudaStream_t st)
+                            size_t pstride, cudaStream_t st, const unsigned* map)
 {
-    k_pyr_down<<<dim3(blocks_for(R * C), pairs), kBlock, 0, st>>>(prev, R, C, out, fovh, pstride);
+    k_pyr_down<<<dim3(blocks_for(R * C), pairs), kBlock, 0, st>>>(prev, R, C, out, fovh, pstride, map);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pyr_copy(PyrLevel src, PyrLevel dst, unsigned n, unsigned pairs, size_t pstride,
+                            const unsigned* map, cudaStream_t st)
+{
+    k_pyr_copy<<<dim3(blocks_for((n + 3) / 4), pairs), kBlock, 0, st>>>(src, dst, n, pstride, map);
     return cudaGetLastError();
 }
 
 static dim3 level_grid(const LevelGeom& g) { return dim3(blocks_for(g.N), g.pairs); }
 
 cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel old_l, PyrLevel new_l,
-                              LevelConsts L, State S, cudaStream_t st)
+                              LevelConsts L, State S, cudaStream_t st, const float* seed)
 {
-    k_level_init<<<level_grid(g), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S);
+    k_level_init<<<level_grid(g), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S, seed);
     return cudaGetLastError();
 }
 
@@ -595,6 +677,18 @@ cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts 
                           float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st)
 {
     k_median<<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, out, dx, dy, dz, p, sel);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L, cudaStream_t st)
+{
+    k_energy_prep<<<level_grid(g), kBlock, 0, st>>>(g, sol, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, cudaStream_t st)
+{
+    k_energy<<<dim3(1, g.pairs), 1024, 0, st>>>(g, sol, L, p, energies);
     return cudaGetLastError();
 }
 

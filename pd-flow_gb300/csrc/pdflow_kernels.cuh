@@ -41,7 +41,14 @@ struct LevelGeom {
     unsigned R, C, N;
     unsigned pairs = 1;
     size_t pstride = 0;
+    const unsigned* map = nullptr;   // device [pairs]: arena slot of grid index y (null: slot y)
 };
+
+// Byte offset of the arena slot that grid index y works on.
+__device__ __forceinline__ size_t pair_off(const unsigned* map, size_t pstride, unsigned y)
+{
+    return (size_t)(map ? __ldg(map + y) : y) * pstride;
+}
 
 template <class T>
 __host__ __device__ __forceinline__ T* at(T* p, size_t off)
@@ -84,14 +91,27 @@ struct Params {
 // ---- launchers (each returns the launch error) ----
 // Pyramid launchers: `pairs` frames, pair k's arena buffers k * pstride bytes
 // after pair 0's; the raw inputs of launch_decode_u16 are [pairs][H][W].
+// A non-null `map` ([pairs] arena slots, device) redirects input k to slot map[k].
 cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
-                              float fovh, unsigned pairs, size_t pstride, cudaStream_t st);
+                              float fovh, unsigned pairs, size_t pstride, cudaStream_t st,
+                              const unsigned* map = nullptr);
 cudaError_t launch_pyr_level0(const float* I, const float* Z, unsigned R, unsigned C, PyrLevel out, float fovh,
-                              unsigned pairs, size_t pstride, cudaStream_t st);
+                              unsigned pairs, size_t pstride, cudaStream_t st, const unsigned* map = nullptr);
 cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, unsigned pairs,
-                            size_t pstride, cudaStream_t st);
+                            size_t pstride, cudaStream_t st, const unsigned* map = nullptr);
+// Copies the planes of `src` over `dst` for the mapped slots (frame t becomes t-1).
+cudaError_t launch_pyr_copy(PyrLevel src, PyrLevel dst, unsigned n, unsigned pairs, size_t pstride,
+                            const unsigned* map, cudaStream_t st);
+// `seed` (device, [pairs][3][N]: du, dv, dw in this level's pixels / metres)
+// replaces the upsampled coarser solution; the duals then start at zero.
 cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel old_l, PyrLevel new_l,
-                              LevelConsts L, State S, cudaStream_t st);
+                              LevelConsts L, State S, cudaStream_t st, const float* seed = nullptr);
+// Energy of the level's solution `sol` (total du, dv in pixels, dw in metres),
+// for the warp point set by launch_energy_prep + gradients + warping:
+// sum over pixels of |dct| + mu |ddt - dw| + lambda_i (|r grad du| + |r grad dv|)
+// + lambda_d |r grad dw|; energies[y] for grid index y.
+cudaError_t launch_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L, cudaStream_t st);
+cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, cudaStream_t st);
 cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st);
 cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p,
                               cudaStream_t st);

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/pdflow.h"
 #include "pdflow_internal.h"
@@ -134,18 +135,31 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     s->stage_u16 = static_cast<uint16_t*>(cv.bytes(Nimg * 2 * s->batch));
     s->flags = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 1024));
     s->status = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 4));
+    s->map = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * s->batch));
+    s->energy = static_cast<float*>(cv.bytes(sizeof(float) * 2 * s->batch));
+    s->seed = (s->ctf_levels > kSeedLevel) || s->rows == 60 ? cv.plane(size_t(3) * kSeedN * s->batch) : nullptr;
     *used = cv.off;
 }
 
-int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs)
+int set_error_code(int code, const char* what, cudaError_t e) { return set_error(code, what, e); }
+
+int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs, const unsigned* map)
 {
     const int f = s->new_slot;
     for (unsigned l = 1; l < s->pyr_levels; ++l) {
         const unsigned Cl = 640 / (s->cam_mode << l), Rl = 480 / (s->cam_mode << l);
-        CUDA_TRY(launch_pyr_down(s->pyr[f][l - 1], Rl, Cl, s->pyr[f][l], s->prm.fovh, pairs, s->pair_stride, st),
+        CUDA_TRY(launch_pyr_down(s->pyr[f][l - 1], Rl, Cl, s->pyr[f][l], s->prm.fovh, pairs, s->pair_stride, st,
+                                 map),
                  "pyramid launch");
     }
     return PDFLOW_OK;
+}
+
+unsigned scaled_iters(unsigned iters, float scale)
+{
+    if (scale >= 1.f) return iters;
+    const double v = std::ceil(double(iters) * double(scale));
+    return v < 0 ? 0u : unsigned(v);
 }
 
 LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, unsigned pairs)
@@ -238,20 +252,44 @@ int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, 
     return enqueue_iterations(s, st, g, s->pyr[s->new_slot ^ 1][li], iters, pairs, &fin, &cnt);
 }
 
-int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs)
+// Energy of level `level`'s median output (the solution passed to the next
+// level): warp both frames at the solution's flow, then sum the data and TV
+// terms per pair into out[0..pairs).
+int enqueue_energy(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, float* out,
+                   const unsigned* map)
+{
+    Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
+    unsigned li;
+    LevelGeom g = level_geom(s, level, &li, pairs);
+    g.map = map;
+    const PyrLevel o = s->pyr[s->new_slot ^ 1][li], n = s->pyr[s->new_slot][li];
+    CUDA_TRY(launch_energy_prep(g, s->sol, s->L, st), "energy prep launch");
+    CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
+    CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
+    CUDA_TRY(launch_energy(g, s->sol, s->L, p, out, st), "energy launch");
+    s->launches += 4;
+    return PDFLOW_OK;
+}
+
+// Levels [plan.first, plan.last] of the coarse-to-fine schedule for pairs
+// [0, pairs) (or the mapped slots).  The plain solve is the default plan.
+int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const SolvePlan& plan)
 {
     Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
     const int fn = s->new_slot, fo = fn ^ 1;
     unsigned count = 0;
-    for (unsigned i = 0; i < s->ctf_levels; ++i) {
+    const unsigned last = plan.last < s->ctf_levels ? plan.last : s->ctf_levels - 1;
+    for (unsigned i = plan.first; i <= last; ++i) {
         unsigned li;
-        const LevelGeom g = level_geom(s, i, &li, pairs);
+        LevelGeom g = level_geom(s, i, &li, pairs);
+        g.map = plan.map;
         const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];
-        CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st), "level init launch");
+        const float* seed = (i == plan.first) ? plan.seed : nullptr;
+        CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st, seed), "level init launch");
         CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
         CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
         count += 3;
-        const unsigned iters = s->prm.num_max_iter[i];
+        const unsigned iters = scaled_iters(s->prm.num_max_iter[i], plan.iter_scale);
         State fin;
         int rc = enqueue_iterations(s, st, g, o, iters, pairs, &fin, &count);
         if (rc) return rc;
@@ -262,8 +300,45 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs)
         CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
                  "median launch");
         ++count;
+        if (int(i) == plan.energy_level && plan.energy) {
+            s->launches = 0;
+            rc = enqueue_energy(s, st, pairs, i, plan.energy, plan.map);
+            if (rc) return rc;
+            count += s->launches;
+        }
     }
     s->launches = count;
+    return PDFLOW_OK;
+}
+
+int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx)
+{
+    if (!s->use_graph) return fn(s, s->stream, pairs, ctx);
+    cudaGraphExec_t ge = nullptr;
+    for (auto& g : s->graphs)
+        if (g.slot == s->new_slot && g.pairs == pairs && g.form == s->iter_form && g.kind == kind) {
+            ge = g.exec;
+            s->launches = g.launches;
+        }
+    if (!ge) {
+        cudaStream_t cap;
+        CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        int rc = PDFLOW_OK;
+        if (e == cudaSuccess) {
+            rc = fn(s, cap, pairs, ctx);
+            cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess && rc == PDFLOW_OK) e = cudaGraphInstantiate(&ge, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cap);
+        if (rc != PDFLOW_OK) return rc;
+        if (e != cudaSuccess) return set_error(PDFLOW_ERR_CUDA, "solve graph capture", e);
+        s->graphs.push_back(pdflow_solver::GraphEntry{s->new_slot, pairs, s->iter_form, kind, ge, s->launches});
+    }
+    CUDA_TRY(cudaGraphLaunch(ge, s->stream), "solve graph launch");
     return PDFLOW_OK;
 }
 
@@ -283,6 +358,34 @@ int push_common(pdflow_solver* s, unsigned pairs)
 }
 
 bool bad_count(const pdflow_solver* s, unsigned n) { return n == 0 || n > s->batch; }
+
+constexpr unsigned kKindPlain = 0, kKindSlots = 1;
+
+int plain_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void*)
+{
+    return enqueue_solve(s, st, pairs);
+}
+
+int slots_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void*)
+{
+    SolvePlan plan;
+    plan.map = s->map;
+    return enqueue_solve(s, st, pairs, plan);
+}
+
+// Checks a slot list (in range, no repeats) and uploads it to the device map.
+int upload_slots(pdflow_solver* s, unsigned n, const unsigned* slots)
+{
+    if (!slots) return set_error(PDFLOW_ERR_ARG, "null slot list");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    std::vector<unsigned char> seen(s->batch, 0);
+    for (unsigned k = 0; k < n; ++k) {
+        if (slots[k] >= s->batch) return set_error(PDFLOW_ERR_ARG, "slot out of range");
+        if (seen[slots[k]]++) return set_error(PDFLOW_ERR_ARG, "slot listed twice");
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->map, slots, sizeof(unsigned) * n, cudaMemcpyHostToDevice, s->stream), "H2D slots");
+    return PDFLOW_OK;
+}
 
 }  // namespace
 
@@ -390,6 +493,7 @@ size_t pdflow_device_bytes(const pdflow_solver* s) { return s ? s->arena_bytes :
 int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float* Z)
 {
     if (!s || !I || !Z) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     const size_t b = size_t(s->width) * s->height * 4;
     s->new_slot ^= 1;  // copyNewFrames pointer swap (pdflow_cudalib.cu:203-221)
@@ -408,6 +512,7 @@ int pdflow_push_frame(pdflow_solver* s, const float* I, const float* Z) { return
 int pdflow_push_frames_u16_device(pdflow_solver* s, unsigned n, const uint8_t* d_intensity, const uint16_t* d_depth)
 {
     if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     s->new_slot ^= 1;
     CUDA_TRY(launch_decode_u16(d_intensity, d_depth, s->width, s->height, s->pyr[s->new_slot][0], s->prm.fovh, n,
@@ -440,34 +545,9 @@ int pdflow_solve_batch(pdflow_solver* s, unsigned n)
 {
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use pdflow_solve_slots");
     if (s->frames < 2) return set_error(PDFLOW_ERR_STATE, "solve needs two pushed frames");
-    if (!s->use_graph) return enqueue_solve(s, s->stream, n);
-    cudaGraphExec_t ge = nullptr;
-    for (auto& g : s->graphs)
-        if (g.slot == s->new_slot && g.pairs == n && g.form == s->iter_form) {
-            ge = g.exec;
-            s->launches = g.launches;
-        }
-    if (!ge) {
-        cudaStream_t cap;
-        CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        int rc = PDFLOW_OK;
-        if (e == cudaSuccess) {
-            rc = enqueue_solve(s, cap, n);
-            cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
-            if (e == cudaSuccess) e = e2;
-        }
-        if (e == cudaSuccess && rc == PDFLOW_OK) e = cudaGraphInstantiate(&ge, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        cudaStreamDestroy(cap);
-        if (rc != PDFLOW_OK) return rc;
-        if (e != cudaSuccess) return set_error(PDFLOW_ERR_CUDA, "solve graph capture", e);
-        s->graphs.push_back(pdflow_solver::GraphEntry{s->new_slot, n, s->iter_form, ge, s->launches});
-    }
-    CUDA_TRY(cudaGraphLaunch(ge, s->stream), "solve graph launch");
-    return PDFLOW_OK;
+    return run_graphed(s, n, kKindPlain, plain_solve, nullptr);
 }
 
 int pdflow_solve(pdflow_solver* s) { return pdflow_solve_batch(s, 1); }
@@ -534,6 +614,91 @@ int pdflow_set_graph_mode(pdflow_solver* s, int use_graph)
 {
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
     s->use_graph = use_graph ? 1 : 0;
+    return PDFLOW_OK;
+}
+
+int pdflow_push_frames_slots_u16_device(pdflow_solver* s, unsigned n, const unsigned* slots,
+                                        const uint8_t* d_intensity, const uint16_t* d_depth)
+{
+    if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (!s->slot_mode && s->frames > 0)
+        return set_error(PDFLOW_ERR_STATE, "frames were pushed for the whole batch: use the batch calls");
+    int rc = upload_slots(s, n, slots);
+    if (rc) return rc;
+    if (s->slot_frames.size() != s->batch) s->slot_frames.assign(s->batch, 0);
+    s->slot_mode = 1;
+    // frame t-1 := frame t for these slots, then frame t := the new frame
+    const int fn = s->new_slot, fo = fn ^ 1;
+    const size_t Nimg = size_t(s->width) * s->height;
+    for (unsigned l = 0; l < s->pyr_levels; ++l)
+        CUDA_TRY(launch_pyr_copy(s->pyr[fn][l], s->pyr[fo][l], unsigned(Nimg >> (2 * l)), n, s->pair_stride, s->map,
+                                 s->stream),
+                 "pyramid copy launch");
+    CUDA_TRY(launch_decode_u16(d_intensity, d_depth, s->width, s->height, s->pyr[fn][0], s->prm.fovh, n,
+                               s->pair_stride, s->stream, s->map),
+             "decode launch");
+    rc = enqueue_pyramid(s, s->stream, n, s->map);
+    if (rc) return rc;
+    for (unsigned k = 0; k < n; ++k)
+        if (s->slot_frames[slots[k]] < 2) ++s->slot_frames[slots[k]];
+    return PDFLOW_OK;
+}
+
+int pdflow_push_frames_slots_u16(pdflow_solver* s, unsigned n, const unsigned* slots, const uint8_t* intensity,
+                                 const uint16_t* depth)
+{
+    if (!s || !intensity || !depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t px = size_t(s->width) * s->height * n;
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u8, intensity, px, cudaMemcpyHostToDevice, s->stream), "H2D intensity");
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u16, depth, px * 2, cudaMemcpyHostToDevice, s->stream), "H2D depth");
+    return pdflow_push_frames_slots_u16_device(s, n, slots, s->stage_u8, s->stage_u16);
+}
+
+int pdflow_solve_slots(pdflow_solver* s, unsigned n, const unsigned* slots)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (!s->slot_mode) return set_error(PDFLOW_ERR_STATE, "no frames were pushed per slot");
+    int rc = upload_slots(s, n, slots);
+    if (rc) return rc;
+    for (unsigned k = 0; k < n; ++k)
+        if (s->slot_frames[slots[k]] < 2) return set_error(PDFLOW_ERR_STATE, "a slot has fewer than two frames");
+    return run_graphed(s, n, kKindSlots, slots_solve, nullptr);
+}
+
+int pdflow_read_flow_slots(pdflow_solver* s, unsigned n, const unsigned* slots, float* dx, float* dy, float* dz)
+{
+    if (!s || !slots || !dx || !dy || !dz) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t N = size_t(s->rows) * s->cols;
+    for (unsigned k = 0; k < n; ++k) {
+        if (slots[k] >= s->batch) return set_error(PDFLOW_ERR_ARG, "slot out of range");
+        const size_t po = slots[k] * s->pair_stride;
+        CUDA_TRY(cudaMemcpyAsync(dx + k * N, at(s->dx, po), N * 4, cudaMemcpyDeviceToHost, s->stream), "D2H dx");
+        CUDA_TRY(cudaMemcpyAsync(dy + k * N, at(s->dy, po), N * 4, cudaMemcpyDeviceToHost, s->stream), "D2H dy");
+        CUDA_TRY(cudaMemcpyAsync(dz + k * N, at(s->dz, po), N * 4, cudaMemcpyDeviceToHost, s->stream), "D2H dz");
+    }
+    return check_status(s);
+}
+
+int pdflow_energy_batch(pdflow_solver* s, unsigned n, float* energies)
+{
+    if (!s || !energies) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    s->launches = 0;
+    int rc = enqueue_energy(s, s->stream, n, s->ctf_levels - 1, s->energy, nullptr);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(energies, s->energy, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream),
+             "D2H energies");
+    return check_status(s);
+}
+
+int pdflow_image_flow_device(pdflow_solver* s, const float** du, const float** dv, const float** dw)
+{
+    if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (du) *du = s->sol.du;
+    if (dv) *dv = s->sol.dv;
+    if (dw) *dw = s->sol.dw;
     return PDFLOW_OK;
 }
 

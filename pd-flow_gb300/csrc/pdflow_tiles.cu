@@ -55,7 +55,7 @@ static_assert(kTX * kTY == kTileThreads && kTY * kPerThread == kRU, "tile thread
 __global__ void __launch_bounds__(kTileThreads, 1) k_iterate_tiles(TileArgs a)
 {
     extern __shared__ float sm[];
-    const size_t po = (size_t)blockIdx.y * a.g.pstride;
+    const size_t po = pair_off(a.g.map, a.g.pstride, blockIdx.y);
     const LevelConsts L = at(a.L, po);
     const State src = at(a.src, po), dst = at(a.dst, po);
     const float* depth_old = at(a.depth_old, po);

@@ -71,6 +71,13 @@ _SIGNATURES = {
     "pdflow_last_solve_launches": (ctypes.c_int, [vp, ctypes.POINTER(u32)]),
     "pdflow_time_level_iterations": (ctypes.c_int, [vp, u32, u32, u32, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_stage_median": (ctypes.c_int, [u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "pdflow_push_frames_slots_u16": (ctypes.c_int, [vp, u32, vp, vp, vp]),
+    "pdflow_push_frames_slots_u16_device": (ctypes.c_int, [vp, u32, vp, vp, vp]),
+    "pdflow_solve_slots": (ctypes.c_int, [vp, u32, vp]),
+    "pdflow_read_flow_slots": (ctypes.c_int, [vp, u32, vp, vp, vp, vp]),
+    "pdflow_energy_batch": (ctypes.c_int, [vp, u32, vp]),
+    "pdflow_image_flow_device": (ctypes.c_int, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]),
+    "pdflow_solve_levels": (ctypes.c_int, [vp, u32, u32, u32, vp, ctypes.c_float, ctypes.c_int, vp]),
 }
 
 
@@ -124,7 +131,74 @@ def _ptr(a: np.ndarray):
     return ctypes.c_void_p(a.ctypes.data)
 
 
-class Solver:
+_cudart_lib = None
+
+
+def _cudart():
+    """The CUDA runtime the library links (already loaded with it)."""
+    global _cudart_lib
+    if _cudart_lib is None:
+        load()
+        for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+            try:
+                _cudart_lib = ctypes.CDLL(name)
+                break
+            except OSError:
+                continue
+        if _cudart_lib is None:
+            raise ExtensionMissing("libcudart is not loadable")
+        _cudart_lib.cudaMemcpy.restype = ctypes.c_int
+        _cudart_lib.cudaMemcpy.argtypes = [vp, vp, ctypes.c_size_t, ctypes.c_int]
+    return _cudart_lib
+
+
+def device_to_host(dptr: int, out: np.ndarray) -> np.ndarray:
+    """Blocking copy of out.nbytes bytes from device address dptr into `out`."""
+    rc = _cudart().cudaMemcpy(_ptr(out), ctypes.c_void_p(dptr), out.nbytes, 2)
+    if rc != 0:
+        raise PDFlowError(ERR_CUDA, "cudaMemcpy device->host")
+    return out
+
+
+class _Extras:
+    """Energy, image-plane flow and level-range solves shared by both classes."""
+
+    def energy(self, n: int = 1) -> np.ndarray:
+        """Energy of the last solve's finest-level solution (pdflow_energy_batch)."""
+        e = np.zeros(n, np.float32)
+        check(load().pdflow_energy_batch(self.handle, n, _ptr(e)), "pdflow_energy_batch")
+        return e
+
+    def image_flow(self, n: int = 1):
+        """(du, dv, dw) [n, rows*cols] of the last solve's finest level (pixels, metres)."""
+        ptrs = [vp() for _ in range(3)]
+        check(load().pdflow_image_flow_device(self.handle, *[ctypes.byref(q) for q in ptrs]),
+              "pdflow_image_flow_device")
+        self.synchronize()
+        stride = self.pair_stride()
+        m = self.rows * self.cols
+        out = [np.zeros((n, m), np.float32) for _ in range(3)]
+        for c in range(3):
+            for k in range(n):
+                device_to_host(ptrs[c].value + k * stride, out[c][k])
+        return out
+
+    def pair_stride(self) -> int:
+        cap, st = u32(), ctypes.c_size_t()
+        check(load().pdflow_batch_info(self.handle, ctypes.byref(cap), ctypes.byref(st)), "pdflow_batch_info")
+        return int(st.value)
+
+    def solve_levels(self, n: int, first: int, last: int = 99, seed_dptr: int | None = None,
+                     iter_scale: float = 1.0, energy_level: int = -1):
+        """Levels [first, last] (pdflow_solve_levels); returns the energies of
+        `energy_level`'s solution when energy_level >= 0."""
+        e = np.zeros(n, np.float32)
+        check(load().pdflow_solve_levels(self.handle, n, first, last, ctypes.c_void_p(seed_dptr or 0),
+                                         float(iter_scale), energy_level, _ptr(e)), "pdflow_solve_levels")
+        return e if energy_level >= 0 else None
+
+
+class Solver(_Extras):
     """One PD-Flow solver (C handle).  Method names follow the reference's
     PD_flow_opencv (scene_flow_impair.h:53-115): construct, initializeCUDA,
     createImagePyramidGPU / loadRGBDFrames, solveSceneFlowGPU, dxp/dyp/dzp,
@@ -239,9 +313,11 @@ class Solver:
 PD_flow = Solver
 
 
-class BatchSolver:
+class BatchSolver(_Extras):
     """Many independent pairs of one configuration solved together
-    (pdflow_create_batch).  Frames are pushed as stacks [n, height, width]."""
+    (pdflow_create_batch).  Frames are pushed as stacks [n, height, width].
+    Slot calls (push_slots / solve_slots / read_flow_slots) treat each slot as
+    a camera stream that keeps its previous frame on the device."""
 
     def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
                  use_graph: bool = True, iteration_form: int = 2):
@@ -285,6 +361,29 @@ class BatchSolver:
 
     def synchronize(self):
         check(load().pdflow_synchronize(self._h), "pdflow_synchronize")
+
+    @staticmethod
+    def _slots(slots) -> np.ndarray:
+        return np.ascontiguousarray(np.asarray(slots, dtype=np.uint32).ravel())
+
+    def push_slots(self, slots, intensity: np.ndarray, depth: np.ndarray):
+        sl = self._slots(slots)
+        i8 = np.ascontiguousarray(intensity, np.uint8).reshape(len(sl), self.height, self.width)
+        z16 = np.ascontiguousarray(depth, np.uint16).reshape(i8.shape)
+        check(load().pdflow_push_frames_slots_u16(self._h, len(sl), _ptr(sl), _ptr(i8), _ptr(z16)),
+              "pdflow_push_frames_slots_u16")
+
+    def solve_slots(self, slots):
+        sl = self._slots(slots)
+        check(load().pdflow_solve_slots(self._h, len(sl), _ptr(sl)), "pdflow_solve_slots")
+
+    def read_flow_slots(self, slots):
+        sl = self._slots(slots)
+        m = self.rows * self.cols
+        out = [np.zeros((len(sl), m), np.float32) for _ in range(3)]
+        check(load().pdflow_read_flow_slots(self._h, len(sl), _ptr(sl), *[_ptr(a) for a in out]),
+              "pdflow_read_flow_slots")
+        return out
 
     def close(self):
         if self._h is not None:
