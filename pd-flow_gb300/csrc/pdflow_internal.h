@@ -50,6 +50,7 @@ struct pdflow_solver {
         unsigned pairs;
         int form;
         unsigned kind;                   // which enqueue sequence (plain, slot-mapped, learned ...)
+        const void* key;                 // object the sequence reads (the network), or null
         cudaGraphExec_t exec;
         unsigned launches;
     };
@@ -83,7 +84,8 @@ unsigned scaled_iters(unsigned iters, float scale);
 // Whatever fn reads from ctx is baked into the graph: equal kinds must mean
 // equal ctx contents.
 using EnqueueFn = int (*)(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void* ctx);
-int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx);
+int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx,
+                const void* key = nullptr);
 int set_error_code(int code, const char* what, cudaError_t e = cudaSuccess);
 int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);
 int check_status(pdflow_solver* s);

@@ -311,12 +311,12 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
     return PDFLOW_OK;
 }
 
-int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx)
+int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx, const void* key)
 {
     if (!s->use_graph) return fn(s, s->stream, pairs, ctx);
     cudaGraphExec_t ge = nullptr;
     for (auto& g : s->graphs)
-        if (g.slot == s->new_slot && g.pairs == pairs && g.form == s->iter_form && g.kind == kind) {
+        if (g.slot == s->new_slot && g.pairs == pairs && g.form == s->iter_form && g.kind == kind && g.key == key) {
             ge = g.exec;
             s->launches = g.launches;
         }
@@ -336,7 +336,7 @@ int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, c
         cudaStreamDestroy(cap);
         if (rc != PDFLOW_OK) return rc;
         if (e != cudaSuccess) return set_error(PDFLOW_ERR_CUDA, "solve graph capture", e);
-        s->graphs.push_back(pdflow_solver::GraphEntry{s->new_slot, pairs, s->iter_form, kind, ge, s->launches});
+        s->graphs.push_back(pdflow_solver::GraphEntry{s->new_slot, pairs, s->iter_form, kind, key, ge, s->launches});
     }
     CUDA_TRY(cudaGraphLaunch(ge, s->stream), "solve graph launch");
     return PDFLOW_OK;

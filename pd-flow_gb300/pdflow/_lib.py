@@ -32,6 +32,16 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
+class LearnedOpts(ctypes.Structure):
+    """pdflow_learned_opts (include/pdflow_net.h)."""
+    _fields_ = [("iter_scale", ctypes.c_float), ("energy_margin", ctypes.c_float)]
+
+
+class LearnedReport(ctypes.Structure):
+    """pdflow_learned_report (include/pdflow_net.h)."""
+    _fields_ = [("fallbacks", ctypes.c_uint), ("max_energy_ratio", ctypes.c_float)]
+
+
 DUMP_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int,
                            ctypes.POINTER(ctypes.c_float), ctypes.c_long)
 
@@ -78,6 +88,24 @@ _SIGNATURES = {
     "pdflow_energy_batch": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_image_flow_device": (ctypes.c_int, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]),
     "pdflow_solve_levels": (ctypes.c_int, [vp, u32, u32, u32, vp, ctypes.c_float, ctypes.c_int, vp]),
+    "pdflow_net_create": (ctypes.c_int, [u32, ctypes.c_ulonglong, ctypes.POINTER(vp)]),
+    "pdflow_net_destroy": (ctypes.c_int, [vp]),
+    "pdflow_net_param_count": (ctypes.c_size_t, [vp]),
+    "pdflow_net_get_params": (ctypes.c_int, [vp, vp, ctypes.c_size_t]),
+    "pdflow_net_set_params": (ctypes.c_int, [vp, vp, ctypes.c_size_t]),
+    "pdflow_net_set_stream": (ctypes.c_int, [vp, vp]),
+    "pdflow_net_forward": (ctypes.c_int, [vp, u32, vp, vp]),
+    "pdflow_net_train_step": (ctypes.c_int, [vp, u32, vp, vp, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
+    "pdflow_net_gradients": (ctypes.c_int, [vp, u32, vp, vp, vp, ctypes.POINTER(ctypes.c_float)]),
+    "pdflow_solve_batch_learned": (ctypes.c_int, [vp, u32, vp, ctypes.POINTER(LearnedOpts),
+                                                  ctypes.POINTER(LearnedReport)]),
+    "pdflow_solve_slots_learned": (ctypes.c_int, [vp, u32, vp, vp, ctypes.POINTER(LearnedOpts),
+                                                  ctypes.POINTER(LearnedReport)]),
+    "pdflow_learned_energies": (ctypes.c_int, [vp, u32, vp, vp]),
+    "pdflow_seed_level_inputs": (ctypes.c_int, [vp, u32, vp]),
+    "pdflow_seed_level_labels": (ctypes.c_int, [vp, u32, vp]),
+    "pdflow_gemm_bf16": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int,
+                                        vp, ctypes.c_int, ctypes.c_int, vp]),
 }
 
 
@@ -385,6 +413,31 @@ class BatchSolver(_Extras):
               "pdflow_read_flow_slots")
         return out
 
+    def solve_learned(self, n: int, net: "Net", iter_scale: float = 0.5, energy_margin: float = 0.01):
+        """Learned warm-start solve of pairs [0, n) (pdflow_solve_batch_learned)."""
+        o, r = LearnedOpts(iter_scale, energy_margin), LearnedReport()
+        check(load().pdflow_solve_batch_learned(self._h, n, net.handle, ctypes.byref(o), ctypes.byref(r)),
+              "pdflow_solve_batch_learned")
+        return dict(fallbacks=r.fallbacks, max_energy_ratio=r.max_energy_ratio)
+
+    def solve_slots_learned(self, slots, net: "Net", iter_scale: float = 0.5, energy_margin: float = 0.01):
+        sl = self._slots(slots)
+        o, r = LearnedOpts(iter_scale, energy_margin), LearnedReport()
+        check(load().pdflow_solve_slots_learned(self._h, len(sl), _ptr(sl), net.handle, ctypes.byref(o),
+                                                ctypes.byref(r)), "pdflow_solve_slots_learned")
+        return dict(fallbacks=r.fallbacks, max_energy_ratio=r.max_energy_ratio)
+
+    def seed_level_inputs(self, n: int, d_out: int):
+        check(load().pdflow_seed_level_inputs(self._h, n, vp(d_out)), "pdflow_seed_level_inputs")
+
+    def seed_level_labels(self, n: int, d_out: int):
+        check(load().pdflow_seed_level_labels(self._h, n, vp(d_out)), "pdflow_seed_level_labels")
+
+    def learned_energies(self, n: int):
+        a, b = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        check(load().pdflow_learned_energies(self._h, n, _ptr(a), _ptr(b)), "pdflow_learned_energies")
+        return a, b
+
     def close(self):
         if self._h is not None:
             load().pdflow_destroy(self._h)
@@ -395,3 +448,64 @@ class BatchSolver(_Extras):
             self.close()
         except Exception:
             pass
+
+
+class Net:
+    """The warm-start network (include/pdflow_net.h).  Device buffers are
+    passed as integer device addresses (e.g. torch's data_ptr())."""
+
+    def __init__(self, max_batch: int, seed: int = 1):
+        h = ctypes.c_void_p()
+        check(load().pdflow_net_create(max_batch, seed, ctypes.byref(h)), "pdflow_net_create")
+        self._h = h
+        self.max_batch = max_batch
+
+    @property
+    def handle(self):
+        return self._h
+
+    def param_count(self) -> int:
+        return int(load().pdflow_net_param_count(self._h))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        check(load().pdflow_net_get_params(self._h, _ptr(p), p.size), "pdflow_net_get_params")
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        check(load().pdflow_net_set_params(self._h, _ptr(p), p.size), "pdflow_net_set_params")
+
+    def forward(self, n: int, d_input: int, d_output: int):
+        check(load().pdflow_net_forward(self._h, n, vp(d_input), vp(d_output)), "pdflow_net_forward")
+
+    def train_step(self, n: int, d_input: int, d_label: int, lr: float) -> float:
+        loss = ctypes.c_float()
+        check(load().pdflow_net_train_step(self._h, n, vp(d_input), vp(d_label), lr, ctypes.byref(loss)),
+              "pdflow_net_train_step")
+        return float(loss.value)
+
+    def gradients(self, n: int, d_input: int, d_label: int):
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_float()
+        check(load().pdflow_net_gradients(self._h, n, vp(d_input), vp(d_label), _ptr(g), ctypes.byref(loss)),
+              "pdflow_net_gradients")
+        return float(loss.value), g
+
+    def close(self):
+        if self._h is not None:
+            load().pdflow_net_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def gemm_bf16(M: int, N: int, K: int, d_a: int, lda: int, d_b: int, ldb: int, d_c: int, ldc: int,
+              k_per_split: int = 0, stream: int = 0):
+    """C = A * B^T on the tcgen05 tensor cores (pdflow_gemm_bf16)."""
+    check(load().pdflow_gemm_bf16(M, N, K, vp(d_a), lda, vp(d_b), ldb, vp(d_c), ldc, k_per_split, vp(stream)),
+          "pdflow_gemm_bf16")

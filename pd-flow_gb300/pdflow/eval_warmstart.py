@@ -1,0 +1,125 @@
+"""Judges the learned warm start against the plain solver on held-out pairs.
+
+    python -m pdflow.eval_warmstart --weights warmstart.npz --rows 480 --pairs 64 --scales 0.5
+
+For each iteration scale it solves the same batch four ways and reports, per
+way, the end-point error against the plain result (metres, mean over pixels
+with valid frame-1 depth, then mean / max over pairs), the final energy
+relative to the plain solve's, and the device time of the batch:
+
+* plain      the reference schedule (pdflow_solve_batch);
+* learned    pdflow_solve_batch_learned (network seed at 60x80, scaled
+             iterations, energy fallback);
+* zero-seed  the same schedule started at 60x80 from zero flow (the learned
+             path without its network);
+* scaled     the plain schedule from the coarsest level with every level's
+             iterations scaled (the same iteration budget without a seed);
+* label_seed the scaled schedule from 60x80 seeded with the plain result
+             itself averaged to 60x80 (what a perfect network would predict).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import BatchSolver, Net, scenes_gpu
+
+HW = 4800
+
+
+def epe(a, b, valid):
+    d = np.sqrt((a[0] - b[0]) ** 2 + (a[1] - b[1]) ** 2 + (a[2] - b[2]) ** 2)
+    return np.array([d[k][valid[k]].mean() for k in range(d.shape[0])])
+
+
+def load_weights(path: str) -> np.ndarray:
+    with np.load(path) as f:
+        return np.asarray(f["params"], np.float32)
+
+
+def evaluate(weights, rows: int, pairs: int, scales, seed0: int = 3_000_000, margin: float = 0.01, log=print):
+    import torch
+
+    vga = rows == 480
+    w, h = (640, 480) if vga else (320, 240)
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(seed0)
+    seeds = list(range(seed0, seed0 + pairs))
+    nobj = {s: int(rng.integers(1, 9)) for s in seeds}
+    i1, z1, i2, z2 = scenes_gpu.make_pairs(torch, seeds, vga, dev, n_objects=lambda s: nobj[s])
+    valid = (z1.cpu().numpy().view(np.uint16) > 0).transpose(0, 2, 1).reshape(pairs, -1)
+    if rows != h:
+        raise ValueError("rows must equal the image height (240 for QVGA, 480 for VGA)")
+    net = Net(pairs, seed=1)
+    net.set_params(weights)
+    b = BatchSolver(rows, w, h, pairs)
+
+    def push():
+        b.push_raw_device(pairs, i1.data_ptr(), z1.data_ptr())
+        b.push_raw_device(pairs, i2.data_ptr(), z2.data_ptr())
+
+    def timed(fn, reps=3):
+        fn()
+        b.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            t = time.perf_counter()
+            r = fn()
+            b.synchronize()
+            best = min(best, time.perf_counter() - t)
+        return r, best
+
+    push()
+    _, t_plain = timed(lambda: b.solve(pairs))
+    plain = b.read_flow(pairs)
+    e_plain = b.energy(pairs)
+    label = torch.zeros((pairs, 3, HW), dtype=torch.float32, device=dev)
+    b.seed_level_labels(pairs, label.data_ptr())
+    out = dict(rows=rows, pairs=pairs, plain_ms=t_plain * 1e3, plain_pairs_s=pairs / t_plain, scales={})
+    zero_seed = torch.zeros((pairs, 3, HW), dtype=torch.float32, device=dev)
+    for s in scales:
+        rep, t_l = timed(lambda: b.solve_learned(pairs, net, s, margin))
+        learned = b.read_flow(pairs)
+        e_l = b.energy(pairs)
+        ep_l = epe(learned, plain, valid)
+        b.solve_levels(pairs, 2, 99, zero_seed.data_ptr(), s)
+        zs = b.read_flow(pairs)
+        e_z = b.energy(pairs)
+        b.solve_levels(pairs, 0, 99, None, s)
+        sc = b.read_flow(pairs)
+        e_s = b.energy(pairs)
+        b.solve_levels(pairs, 2, 99, label.data_ptr(), s)
+        ls = b.read_flow(pairs)
+        e_ls = b.energy(pairs)
+        r = dict(learned_ms=t_l * 1e3, learned_pairs_s=pairs / t_l, fallbacks=rep["fallbacks"],
+                 max_seed_energy_ratio=rep["max_energy_ratio"])
+        for name, flow, en in (("learned", learned, e_l), ("zero_seed", zs, e_z), ("scaled", sc, e_s),
+                               ("label_seed", ls, e_ls)):
+            ep = ep_l if name == "learned" else epe(flow, plain, valid)
+            r[name] = dict(epe_mean_m=float(ep.mean()), epe_max_pair_m=float(ep.max()),
+                           energy_ratio_mean=float((en / e_plain).mean()), energy_ratio_max=float((en / e_plain).max()))
+        out["scales"][str(s)] = r
+        log(json.dumps({str(s): r}))
+    b.close()
+    net.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--weights", required=True)
+    ap.add_argument("--rows", type=int, default=480, choices=(240, 480))
+    ap.add_argument("--pairs", type=int, default=64)
+    ap.add_argument("--scales", default="0.5")
+    ap.add_argument("--margin", type=float, default=0.01)
+    a = ap.parse_args()
+    res = evaluate(load_weights(a.weights), a.rows, a.pairs, [float(x) for x in a.scales.split(",")],
+                   margin=a.margin)
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
