@@ -172,6 +172,29 @@ int pdflow_solve_slots(pdflow_solver* s, unsigned n, const unsigned* slots);
 /* Copies the listed slots' motion fields to host arrays [n][rows*cols]. */
 int pdflow_read_flow_slots(pdflow_solver* s, unsigned n, const unsigned* slots, float* dx, float* dy, float* dz);
 
+/* ---- Launch-form autotuner (no counterpart in the reference) ----
+ * A level's iterations can run as two kernels per iteration (form 0), one
+ * persistent launch per level (form 1: one CTA, a cluster, or, for a single
+ * pair, the cooperative grid) or temporally blocked shared-memory tiles with
+ * 2..4 iterations per launch (form 2; the iterations between two grid-wide
+ * synchronisations).  pdflow_autotune times every eligible candidate of every
+ * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
+ * 0 = 8) and keeps the fastest per level; all forms give the same bits.  The
+ * handle's solution state is overwritten (the pushed frames are kept). */
+#define PDFLOW_TUNE_CANDIDATES 5      /* form 0, form 1, form 2 x {2, 3, 4} iterations per launch */
+typedef struct pdflow_tune_level {
+    int form;                         /* chosen form */
+    unsigned iters_per_launch;        /* chosen iterations per launch (form 2) */
+    float ms_per_iter[PDFLOW_TUNE_CANDIDATES];   /* per candidate; NaN if not eligible */
+} pdflow_tune_level;
+typedef struct pdflow_tune_report {
+    unsigned levels;
+    pdflow_tune_level level[8];
+} pdflow_tune_report;
+int pdflow_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_tune_report* report);
+/* Sets level `level`'s form by hand (-1 restores the default choice). */
+int pdflow_set_level_form(pdflow_solver* s, unsigned level, int form, unsigned iters_per_launch);
+
 /* ---- Energy of a solution (no counterpart in the reference) ----
  * The functional the iterations minimise, evaluated at the last solve's
  * finest-level solution of pairs [0, n) (blocks; host array [n]):

@@ -29,6 +29,9 @@ typedef struct pdflow_net pdflow_net;
  * weights drawn from `seed` (device buffers for training included). */
 int pdflow_net_create(unsigned max_batch, unsigned long long seed, pdflow_net** out);
 int pdflow_net_destroy(pdflow_net* n);
+/* Device memory the network holds (weights, optimiser state, activation and
+ * gradient buffers for max_batch inputs), in bytes. */
+size_t pdflow_net_device_bytes(const pdflow_net* n);
 
 /* Parameters: FP32, per convolution (in network order) the weights
  * [cout][3*3*cin] (tap-major: tap = 3*dh + dw, then input channel) followed

@@ -33,6 +33,8 @@ struct pdflow_solver {
     unsigned* status = nullptr;          // device status word (0 = ok)
     int num_sms = 0;
     int iter_form = 2;                   // 2 = tiles for large levels, 1 = one launch per level, 0 = two kernels per iteration
+    int level_form[8] = {-1, -1, -1, -1, -1, -1, -1, -1};   // per-level override (autotuner); -1 = iter_form's choice
+    unsigned level_kk[8] = {};           // tile form: iterations per launch (0 = the halo width)
     float* dx = nullptr;
     float* dy = nullptr;
     float* dz = nullptr;

@@ -44,11 +44,13 @@ struct LevelGeom {
     const unsigned* map = nullptr;   // device [pairs]: arena slot of grid index y (null: slot y)
 };
 
+#ifdef __CUDACC__
 // Byte offset of the arena slot that grid index y works on.
 __device__ __forceinline__ size_t pair_off(const unsigned* map, size_t pstride, unsigned y)
 {
     return (size_t)(map ? __ldg(map + y) : y) * pstride;
 }
+#endif
 
 template <class T>
 __host__ __device__ __forceinline__ T* at(T* p, size_t off)

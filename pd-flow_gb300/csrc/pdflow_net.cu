@@ -399,6 +399,7 @@ struct pdflow_net {
     unsigned* status = nullptr;
     size_t col_elems = 0, part_elems = 0;
     int step = 0;
+    size_t device_bytes = 0;
     std::vector<void*> allocs;
 };
 
@@ -529,6 +530,7 @@ T* dalloc(pdflow_net* n, size_t count, cudaError_t* e)
     if (*e == cudaSuccess) *e = cudaMalloc(&p, count * sizeof(T) + 16);
     if (*e == cudaSuccess) {
         n->allocs.push_back(p);
+        n->device_bytes += count * sizeof(T) + 16;
         *e = cudaMemset(p, 0, count * sizeof(T) + 16);
     }
     return static_cast<T*>(p);
@@ -875,6 +877,8 @@ int pdflow_net_destroy(pdflow_net* n)
 }
 
 size_t pdflow_net_param_count(const pdflow_net* n) { return n ? n->nparams : 0; }
+
+size_t pdflow_net_device_bytes(const pdflow_net* n) { return n ? n->device_bytes : 0; }
 
 int pdflow_net_set_params(pdflow_net* n, const float* params, size_t count)
 {

@@ -182,19 +182,28 @@ LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, 
 // solve's launch form; returns the number of kernels launched via *count.
 // The final duals' buffer is reported in *fin.
 static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom& g, const PyrLevel& o,
-                              unsigned iters, unsigned pairs, State* fin, unsigned* count)
+                              unsigned iters, unsigned pairs, State* fin, unsigned* count, unsigned level)
 {
     Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
     *fin = s->S;
     const IterPlan pl = plan_iterate(g, s->num_sms);
-    const bool tiles = s->iter_form == 2 && iters > 0 && pl.mode == kIterGrid && pairs > 1;
-    const bool one_launch = s->iter_form >= 1 && iters > 0 && !tiles && (pairs == 1 || pl.mode != kIterGrid) &&
-                            pl.smem_bytes <= iterate_smem_limit();
+    const int forced = level < 8 ? s->level_form[level] : -1;
+    const bool one_launch_ok = (pairs == 1 || pl.mode != kIterGrid) && pl.smem_bytes <= iterate_smem_limit();
+    bool tiles, one_launch;
+    if (forced >= 0) {
+        tiles = forced == 2 && iters > 0;
+        one_launch = forced == 1 && iters > 0 && one_launch_ok;
+    } else {
+        tiles = s->iter_form == 2 && iters > 0 && pl.mode == kIterGrid && pairs > 1;
+        one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
+    }
     if (tiles) {
         State cur = s->S;
         State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
                   s->alt[5], s->alt[6], s->alt[7], s->alt[8], s->alt[9]};
-        const unsigned h = tiles_halo();
+        const unsigned h = (level < 8 && s->level_kk[level] > 0 && s->level_kk[level] <= tiles_halo())
+                               ? s->level_kk[level]
+                               : tiles_halo();
         for (unsigned done = 0; done < iters;) {
             const unsigned kk = (iters - done < h) ? iters - done : h;
             CUDA_TRY(launch_iterate_tiles(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st),
@@ -249,7 +258,7 @@ int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, 
     unsigned li, cnt = 0;
     const LevelGeom g = level_geom(s, level, &li, pairs);
     State fin;
-    return enqueue_iterations(s, st, g, s->pyr[s->new_slot ^ 1][li], iters, pairs, &fin, &cnt);
+    return enqueue_iterations(s, st, g, s->pyr[s->new_slot ^ 1][li], iters, pairs, &fin, &cnt, level);
 }
 
 // Energy of level `level`'s median output (the solution passed to the next
@@ -291,7 +300,7 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
         count += 3;
         const unsigned iters = scaled_iters(s->prm.num_max_iter[i], plan.iter_scale);
         State fin;
-        int rc = enqueue_iterations(s, st, g, o, iters, pairs, &fin, &count);
+        int rc = enqueue_iterations(s, st, g, o, iters, pairs, &fin, &count, i);
         if (rc) return rc;
         if (iters == 0) {
             CUDA_TRY(launch_saturate(g, s->L, s->S, o.dep, st), "saturate launch");

@@ -42,6 +42,49 @@ class LearnedReport(ctypes.Structure):
     _fields_ = [("fallbacks", ctypes.c_uint), ("max_energy_ratio", ctypes.c_float)]
 
 
+class NoiseTex(ctypes.Structure):
+    """pdflow_noise_tex (include/pdflow_scene.h)."""
+    _fields_ = [("perm", ctypes.c_int32 * 256), ("vals", ctypes.c_double * 256), ("cell", ctypes.c_double)]
+
+
+class SceneObject(ctypes.Structure):
+    """pdflow_scene_object (include/pdflow_scene.h)."""
+    _fields_ = [("kind", ctypes.c_int32), ("pad_", ctypes.c_int32), ("center", ctypes.c_double * 3),
+                ("rot", ctypes.c_double * 9), ("next_center", ctypes.c_double * 3), ("next_rot", ctypes.c_double * 9),
+                ("size", ctypes.c_double * 3), ("albedo", ctypes.c_double), ("tex", NoiseTex)]
+
+
+class SceneFrame(ctypes.Structure):
+    """pdflow_scene_frame (include/pdflow_scene.h)."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("fx", ctypes.c_double),
+                ("fy", ctypes.c_double), ("cx", ctypes.c_double), ("cy", ctypes.c_double),
+                ("plane", ctypes.c_double * 3), ("plane_tex", NoiseTex), ("n_objects", ctypes.c_uint32),
+                ("sensor_noise", ctypes.c_uint32), ("noise_seed", ctypes.c_uint64), ("objects", SceneObject * 8)]
+
+
+class ServerConfig(ctypes.Structure):
+    """pdflow_server_config (include/pdflow_server.h)."""
+    _fields_ = [("device_budget_bytes", ctypes.c_size_t), ("slots_per_lane", ctypes.c_uint), ("learned", ctypes.c_int),
+                ("iter_scale", ctypes.c_float), ("energy_margin", ctypes.c_float),
+                ("net_params", ctypes.POINTER(ctypes.c_float)), ("net_param_count", ctypes.c_size_t)]
+
+
+class RequestInfo(ctypes.Structure):
+    """pdflow_request_info (include/pdflow_server.h)."""
+    _fields_ = [("request_id", ctypes.c_ulonglong), ("stream_id", ctypes.c_uint), ("frame_index", ctypes.c_ulonglong),
+                ("status", ctypes.c_int), ("has_flow", ctypes.c_int), ("batch_pairs", ctypes.c_uint),
+                ("batch_fallbacks", ctypes.c_uint), ("submit_ms", ctypes.c_double), ("start_ms", ctypes.c_double),
+                ("done_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    """pdflow_server_stats (include/pdflow_server.h)."""
+    _fields_ = [("lanes", ctypes.c_uint), ("streams", ctypes.c_uint), ("submitted", ctypes.c_ulonglong),
+                ("completed", ctypes.c_ulonglong), ("batches", ctypes.c_ulonglong),
+                ("pairs_solved", ctypes.c_ulonglong), ("fallbacks", ctypes.c_ulonglong),
+                ("device_bytes", ctypes.c_size_t)]
+
+
 DUMP_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int,
                            ctypes.POINTER(ctypes.c_float), ctypes.c_long)
 
@@ -102,6 +145,16 @@ _SIGNATURES = {
     "pdflow_solve_slots_learned": (ctypes.c_int, [vp, u32, vp, vp, ctypes.POINTER(LearnedOpts),
                                                   ctypes.POINTER(LearnedReport)]),
     "pdflow_learned_energies": (ctypes.c_int, [vp, u32, vp, vp]),
+    "pdflow_render_frames": (ctypes.c_int, [ctypes.POINTER(SceneFrame), u32, vp, vp, vp, vp]),
+    "pdflow_net_device_bytes": (ctypes.c_size_t, [vp]),
+    "pdflow_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),
+    "pdflow_server_destroy": (ctypes.c_int, [vp]),
+    "pdflow_server_open_stream": (ctypes.c_int, [vp, u32, u32, ctypes.POINTER(u32)]),
+    "pdflow_server_close_stream": (ctypes.c_int, [vp, u32]),
+    "pdflow_server_submit": (ctypes.c_int, [vp, u32, vp, vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "pdflow_server_wait": (ctypes.c_int, [vp, ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(RequestInfo), vp, vp,
+                                          vp]),
+    "pdflow_server_get_stats": (ctypes.c_int, [vp, ctypes.POINTER(ServerStats)]),
     "pdflow_seed_level_inputs": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_seed_level_labels": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_gemm_bf16": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int,
@@ -502,6 +555,23 @@ class Net:
             self.close()
         except Exception:
             pass
+
+
+def render_frames(frames, d_intensity: int, d_depth: int, d_flow: int | None = None, stream: int = 0):
+    """Renders SceneFrame descriptors into device buffers (pdflow_render_frames)."""
+    arr = (SceneFrame * len(frames))(*frames)
+    check(load().pdflow_render_frames(arr, len(frames), vp(d_intensity), vp(d_depth), vp(d_flow or 0), vp(stream)),
+          "pdflow_render_frames")
+
+
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "warmstart.npz")
+
+
+def load_weights(path: str | None = None) -> np.ndarray:
+    """Parameters of the warm-start network (default: the shipped weights,
+    trained by pdflow.train_warmstart on 20 000 synthetic pairs)."""
+    with np.load(path or DEFAULT_WEIGHTS) as f:
+        return np.asarray(f["params"], np.float32)
 
 
 def gemm_bf16(M: int, N: int, K: int, d_a: int, lda: int, d_b: int, ldb: int, d_c: int, ldc: int,

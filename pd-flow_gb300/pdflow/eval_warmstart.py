@@ -2,10 +2,11 @@
 
     python -m pdflow.eval_warmstart --weights warmstart.npz --rows 480 --pairs 64 --scales 0.5
 
-For each iteration scale it solves the same batch four ways and reports, per
-way, the end-point error against the plain result (metres, mean over pixels
-with valid frame-1 depth, then mean / max over pairs), the final energy
-relative to the plain solve's, and the device time of the batch:
+For each iteration scale it solves the same batch several ways and reports,
+per way, the end-point error against the plain result and against the
+scenes' ground-truth motion (metres, mean over pixels with valid frame-1
+depth, then mean / max over pairs), the final energy relative to the plain
+solve's, and the time of the batch:
 
 * plain      the reference schedule (pdflow_solve_batch);
 * learned    pdflow_solve_batch_learned (network seed at 60x80, scaled
@@ -25,7 +26,7 @@ import time
 
 import numpy as np
 
-from . import BatchSolver, Net, scenes_gpu
+from . import BatchSolver, Net, datagen
 
 HW = 4800
 
@@ -49,8 +50,10 @@ def evaluate(weights, rows: int, pairs: int, scales, seed0: int = 3_000_000, mar
     rng = np.random.default_rng(seed0)
     seeds = list(range(seed0, seed0 + pairs))
     nobj = {s: int(rng.integers(1, 9)) for s in seeds}
-    i1, z1, i2, z2 = scenes_gpu.make_pairs(torch, seeds, vga, dev, n_objects=lambda s: nobj[s])
+    i1, z1, i2, z2, gt = datagen.render_pairs(torch, seeds, vga, n_objects=lambda s: nobj[s], with_flow=True)
     valid = (z1.cpu().numpy().view(np.uint16) > 0).transpose(0, 2, 1).reshape(pairs, -1)
+    gt = gt.cpu().numpy()
+    gt = [gt[:, 0], gt[:, 1], gt[:, 2]]
     if rows != h:
         raise ValueError("rows must equal the image height (240 for QVGA, 480 for VGA)")
     net = Net(pairs, seed=1)
@@ -78,7 +81,9 @@ def evaluate(weights, rows: int, pairs: int, scales, seed0: int = 3_000_000, mar
     e_plain = b.energy(pairs)
     label = torch.zeros((pairs, 3, HW), dtype=torch.float32, device=dev)
     b.seed_level_labels(pairs, label.data_ptr())
-    out = dict(rows=rows, pairs=pairs, plain_ms=t_plain * 1e3, plain_pairs_s=pairs / t_plain, scales={})
+    ep_gt_plain = epe(plain, gt, valid)
+    out = dict(rows=rows, pairs=pairs, plain_ms=t_plain * 1e3, plain_pairs_s=pairs / t_plain,
+               plain_epe_gt_m=float(ep_gt_plain.mean()), scales={})
     zero_seed = torch.zeros((pairs, 3, HW), dtype=torch.float32, device=dev)
     for s in scales:
         rep, t_l = timed(lambda: b.solve_learned(pairs, net, s, margin))
@@ -100,6 +105,7 @@ def evaluate(weights, rows: int, pairs: int, scales, seed0: int = 3_000_000, mar
                                ("label_seed", ls, e_ls)):
             ep = ep_l if name == "learned" else epe(flow, plain, valid)
             r[name] = dict(epe_mean_m=float(ep.mean()), epe_max_pair_m=float(ep.max()),
+                           epe_gt_mean_m=float(epe(flow, gt, valid).mean()),
                            energy_ratio_mean=float((en / e_plain).mean()), energy_ratio_max=float((en / e_plain).max()))
         out["scales"][str(s)] = r
         log(json.dumps({str(s): r}))

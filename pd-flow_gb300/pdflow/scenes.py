@@ -193,6 +193,96 @@ def render(scene: Scene, k: int):
     return inten, depth
 
 
+def _tex_desc(tex: _Noise3):
+    from ._lib import NoiseTex
+    t = NoiseTex()
+    t.perm[:] = [int(x) for x in tex.perm]
+    t.vals[:] = [float(x) for x in tex.vals]
+    t.cell = float(tex.cell)
+    return t
+
+
+def frame_desc(scene: Scene, k: int, sensor_noise: bool = True):
+    """The GPU renderer's descriptor (pdflow_scene_frame) of frame k: the same
+    geometry and textures as `render`; the sensor noise comes from the
+    renderer's counter-based generator keyed by (noise_seed, k)."""
+    from ._lib import SceneFrame, SceneObject
+    f = SceneFrame()
+    cam = scene.cam
+    f.width, f.height = cam["width"], cam["height"]
+    f.fx, f.fy, f.cx, f.cy = cam["fx"], cam["fy"], cam["cx"], cam["cy"]
+    f.plane[:] = list(scene.plane)
+    f.plane_tex = _tex_desc(scene.plane_tex)
+    f.n_objects = len(scene.objects)
+    f.sensor_noise = 1 if sensor_noise else 0
+    f.noise_seed = (int(scene.noise_seed) * 1_000_003 + k) & 0xFFFFFFFFFFFFFFFF
+    for j, ob in enumerate(scene.objects):
+        o = SceneObject()
+        o.kind = 0 if ob.kind == "sphere" else 1
+        c, r = ob.pose(k)
+        cn, rn = ob.pose(k + 1)
+        o.center[:] = list(c)
+        o.rot[:] = list(r.ravel())
+        o.next_center[:] = list(cn)
+        o.next_rot[:] = list(rn.ravel())
+        sz = list(ob.size) + [0.0] * (3 - len(ob.size))
+        o.size[:] = sz
+        o.albedo = float(ob.albedo)
+        o.tex = _tex_desc(ob.tex)
+        f.objects[j] = o
+    return f
+
+
+def ground_truth_flow(scene: Scene, k: int) -> np.ndarray:
+    """Motion of each pixel's surface point from frame k to k+1, [3, w*h],
+    in the solver's output convention: dx = depth change, dy = horizontal,
+    dz = vertical (metres), column-major (idx = v + u * height)."""
+    cam = scene.cam
+    w, h = cam["width"], cam["height"]
+    uu, vv = np.meshgrid(np.arange(w, dtype=np.float64), np.arange(h, dtype=np.float64))
+    xn = ((uu - cam["cx"]) / cam["fx"]).ravel()
+    yn = ((vv - cam["cy"]) / cam["fy"]).ravel()
+    d = np.stack([xn, yn, np.ones_like(xn)], axis=1)
+    z0, a, b = scene.plane
+    zbest = z0 / (1.0 - a * xn - b * yn)
+    hit = np.full(xn.shape, -1)
+    for j, ob in enumerate(scene.objects):
+        c, r = ob.pose(k)
+        if ob.kind == "sphere":
+            rad = ob.size[0]
+            dd = np.einsum("ij,ij->i", d, d)
+            dc = d @ c
+            disc = dc * dc - dd * (c @ c - rad * rad)
+            t = np.full_like(xn, np.inf)
+            ok = disc > 0
+            t[ok] = (dc[ok] - np.sqrt(disc[ok])) / dd[ok]
+        else:
+            o_l = r.T @ (-c)
+            d_l = d @ r
+            with np.errstate(divide="ignore", invalid="ignore"):
+                inv = 1.0 / d_l
+                t1 = (-ob.size[None, :] - o_l[None, :]) * inv
+                t2 = (ob.size[None, :] - o_l[None, :]) * inv
+            tn = np.nanmax(np.minimum(t1, t2), axis=1)
+            tf = np.nanmin(np.maximum(t1, t2), axis=1)
+            t = np.where((tn <= tf) & (tf > 0), tn, np.inf)
+        closer = t < zbest
+        zbest = np.where(closer, t, zbest)
+        hit = np.where(closer, j, hit)
+    P = d * zbest[:, None]
+    gt = np.zeros_like(P)
+    for j, ob in enumerate(scene.objects):
+        m = hit == j
+        if not m.any():
+            continue
+        c, r = ob.pose(k)
+        cn, rn = ob.pose(k + 1)
+        L = (P[m] - c[None, :]) @ r
+        gt[m] = L @ rn.T + cn[None, :] - P[m]
+    gt = gt.reshape(h, w, 3).transpose(1, 0, 2).reshape(-1, 3)     # column-major
+    return np.stack([gt[:, 2], gt[:, 0], gt[:, 1]])
+
+
 def make_pair(seed: int, vga: bool = False, n_objects: int | None = None):
     """(I1, Z1, I2, Z2) for `seed`: uint8/uint16 row-major images of frames 0 and 1."""
     sc = make_scene(seed, vga, n_objects)

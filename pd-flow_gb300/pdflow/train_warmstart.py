@@ -12,8 +12,8 @@
    and Adam (cosine learning-rate decay), holding out 5 % for validation;
 4. writes the FP32 parameters and the training record to `--out`.
 
-torch provides device memory and the renderer; every solve, forward, backward
-and update runs in libpdflow_gb300.so.
+torch holds the device buffers; every render, solve, forward, backward and
+update runs in libpdflow_gb300.so.
 """
 from __future__ import annotations
 
@@ -24,7 +24,7 @@ import time
 
 import numpy as np
 
-from . import BatchSolver, Net, scenes_gpu
+from . import BatchSolver, Net, datagen
 
 HW = 4800
 
@@ -46,7 +46,7 @@ def build_dataset(torch, n_pairs: int, batch: int, log):
             nb = min(batch, count - done)
             seeds = [seed0 + done + j for j in range(nb)]
             nobj = {s: int(rng.integers(1, 9)) for s in seeds}
-            i1, z1, i2, z2 = scenes_gpu.make_pairs(torch, seeds, vga, dev, n_objects=lambda s: nobj[s])
+            i1, z1, i2, z2 = datagen.render_pairs(torch, seeds, vga, n_objects=lambda s: nobj[s])
             solver.push_raw_device(nb, i1.data_ptr(), z1.data_ptr())
             solver.push_raw_device(nb, i2.data_ptr(), z2.data_ptr())
             solver.solve(nb)

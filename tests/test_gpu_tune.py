@@ -1,0 +1,48 @@
+"""The launch-form autotuner: every candidate gives the same bits, and the
+tuned handle still solves bit-exactly."""
+import numpy as np
+import pytest
+
+from pdflow import BatchSolver, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotuned_forms_give_the_same_bits(built_lib):
+    import ctypes
+    from pdflow import _lib
+    pairs = [scenes.make_pair(900 + k) for k in range(3)]
+    b = BatchSolver(240, 320, 240, 3)
+    b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
+    b.push_raw(np.stack([p[2] for p in pairs]), np.stack([p[3] for p in pairs]))
+    b.solve(3)
+    ref = b.read_flow(3)
+
+    class Level(ctypes.Structure):
+        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 5)]
+
+    class Report(ctypes.Structure):
+        _fields_ = [("levels", ctypes.c_uint), ("level", Level * 8)]
+
+    lib = _lib.load()
+    lib.pdflow_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(Report)]
+    rep = Report()
+    assert lib.pdflow_autotune(b.handle, 3, 4, ctypes.byref(rep)) == 0
+    assert rep.levels == 5
+    for i in range(rep.levels):
+        assert rep.level[i].form in (0, 1, 2)
+        assert np.isfinite(rep.level[i].ms_per_iter[0])
+    b.solve(3)
+    got = b.read_flow(3)
+    for x, y in zip(got, ref):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    # each tile width of iterations per launch, forced on every level
+    lib.pdflow_set_level_form.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_uint]
+    for kk in (1, 2, 3):
+        for lvl in range(5):
+            assert lib.pdflow_set_level_form(b.handle, lvl, 2, kk) == 0
+        b.solve(3)
+        got = b.read_flow(3)
+        for x, y in zip(got, ref):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    b.close()

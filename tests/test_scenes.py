@@ -50,3 +50,23 @@ def test_decode_matches_reference_packing():
     h, w = i1.shape
     assert I[5 + 7 * h] == i1[5, 7]
     assert Z[5 + 7 * h] == np.float32(z1[5, 7]) * np.float32(1 / 5000)
+
+
+def test_ground_truth_flow_is_zero_on_the_plane_and_bounded_on_objects():
+    sc = scenes.make_scene(12, vga=False, n_objects=4)
+    gt = scenes.ground_truth_flow(sc, 0)
+    assert gt.shape == (3, 320 * 240)
+    mag = np.sqrt((gt ** 2).sum(axis=0))
+    moving = mag > 0
+    assert 0.01 < moving.mean() < 0.9          # objects cover part of the image, the plane is static
+    assert mag.max() < 0.05 + 3 * np.pi / 180 * 0.4   # <= 5 cm translation + 3 deg about a centre <= 0.4 m away
+
+
+def test_ground_truth_flow_of_a_translating_object_is_its_translation():
+    sc = scenes.make_scene(21, vga=False, n_objects=1)
+    ob = sc.objects[0]
+    ob.d_rot = np.eye(3)                      # pure translation
+    gt = scenes.ground_truth_flow(sc, 0)
+    moving = np.sqrt((gt ** 2).sum(axis=0)) > 0
+    dx, dy, dz = ob.d_center[2], ob.d_center[0], ob.d_center[1]   # depth, horizontal, vertical
+    assert np.allclose(gt[0][moving], dx) and np.allclose(gt[1][moving], dy) and np.allclose(gt[2][moving], dz)
