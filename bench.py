@@ -1,19 +1,23 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 PD-Flow solver (one JSON line on stdout).
 
-Workload: VGA scene flow, rows = 480 (640x480 frames, 6 pyramid levels,
-25..100 iterations), seeded synthetic RGB-D pairs (textured plane plus six
-boxes/spheres with rigid motions, depth noise and 2 % holes).  A step is one
+Workload: VGA scene flow, rows = 480 (640x480 frames, 6 pyramid levels),
+seeded synthetic RGB-D pairs (textured plane plus 1-8 boxes/spheres with
+rigid motions, depth noise and 2 % holes) rendered on the GPU.  A step is one
 pass of the hot path over one batch: push both frames of every pair (device
-decode + Gaussian pyramid) and the full coarse-to-fine solve.
+decode + Gaussian pyramid) and the learned warm-started solve (plain levels
+to 60x80, network seed, scaled iterations from 60x80 on, energy fallback).
 
-  value      batched VGA pairs/s, frames resident in HBM (per-step CUDA events
-             on the solver's stream; the batch's working set, ~90 MB per pair,
-             is far larger than L2, so no flush is needed)
+  value      learned + batched VGA pairs/s, frames resident in HBM (per-step
+             CUDA events on the solver's stream; ~90 MB of state per pair, far
+             larger than L2, so no flush is needed)
+  accuracy   end-point error against the plain result and against the scenes'
+             ground-truth motion, energy relative to the plain solve
   e2e        the same through the public C ABI from pinned host buffers: raw
              frames host->device, solve, flow device->host, every step
   plain      one pair at a time (the plain single-pair solver), L2 flushed
              before every step; pairs/s and p50/p99 latency
+  serving    16 simulated cameras through the request loop: p50/p99 latency
   roofline   the dominant kernel: the finest level's iterations, timed alone
   cpu_baseline / --impl reference
              the FP32 C/OpenMP restatement of the reference (oracle/) on the
@@ -197,9 +201,61 @@ def profiled_traffic():
     return None
 
 
+def render_batch(torch, B, seed0=4_000_000):
+    """B distinct seeded VGA pairs (1-8 objects) rendered on the GPU, with the
+    ground-truth motion of frame 1."""
+    from pdflow import datagen
+    rng = np.random.default_rng(seed0)
+    seeds = list(range(seed0, seed0 + B))
+    nobj = {s_: int(rng.integers(1, 9)) for s_ in seeds}
+    return datagen.render_pairs(torch, seeds, True, n_objects=lambda s_: nobj[s_], with_flow=True)
+
+
+def epe(a, b, valid):
+    d = np.sqrt(sum((x - y) ** 2 for x, y in zip(a, b)))
+    return np.array([d[k][valid[k]].mean() for k in range(d.shape[0])])
+
+
+def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
+    """16 camera streams (8 QVGA, 8 VGA) at `rate` Hz with Poisson arrivals
+    through the request loop, learned warm start on."""
+    from pdflow import datagen, scenes
+    from pdflow.serving import Server, simulate
+    T = int(seconds * rate)
+    streams = []
+    for vga in (False, True):
+        scs = [scenes.make_scene(8_000_000 + 100 * vga + j, vga, 3 + j % 4) for j in range(8)]
+        for j, sc in enumerate(scs):
+            frames = []
+            for k0 in range(0, T, 30):
+                ks = list(range(k0, min(T, k0 + 30)))
+                descs = [scenes.frame_desc(sc, k) for k in ks]
+                w, h = sc.width, sc.height
+                ii = torch.empty((len(ks), h, w), dtype=torch.uint8, device="cuda")
+                zz = torch.empty((len(ks), h, w), dtype=torch.int16, device="cuda")
+                from pdflow import render_frames
+                render_frames(descs, ii.data_ptr(), zz.data_ptr(), None, torch.cuda.current_stream().cuda_stream)
+                ih, zh = ii.cpu().numpy(), zz.cpu().numpy().view(np.uint16)
+                frames += [(ih[q], zh[q]) for q in range(len(ks))]
+            streams.append((sc.width, sc.height, frames))
+    srv = Server(device_budget_bytes=64 << 30, slots_per_lane=4, learned=True, iter_scale=iter_scale,
+                 energy_margin=margin, net_params=weights)
+    infos, _, summary = simulate(srv, streams, rate_hz=rate, seed=1)
+    vga_lat = [i["done_ms"] - i["submit_ms"] for i in infos if i["has_flow"] and streams[i["stream_id"]][1] == 480]
+    qvga_lat = [i["done_ms"] - i["submit_ms"] for i in infos if i["has_flow"] and streams[i["stream_id"]][1] == 240]
+    st = srv.stats()
+    srv.close()
+    summary.update(vga_p50_ms=float(np.percentile(vga_lat, 50)), vga_p99_ms=float(np.percentile(vga_lat, 99)),
+                   qvga_p50_ms=float(np.percentile(qvga_lat, 50)), qvga_p99_ms=float(np.percentile(qvga_lat, 99)),
+                   lanes=st["lanes"], batches=st["batches"], device_bytes=st["device_bytes"],
+                   streams_desc="8 QVGA rows=240 + 8 VGA rows=480, Poisson arrivals at 30 Hz each, "
+                                f"{seconds:.0f} s of frames")
+    return summary
+
+
 def ours(args):
     import torch
-    from pdflow import BatchSolver, Solver, _lib
+    from pdflow import BatchSolver, Net, Solver, _lib, load_weights
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -210,27 +266,46 @@ def ours(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     B, K, W = args.batch, args.steps, args.warmup
-    log(f"[rank {rank}] generating {min(B, 16)} distinct VGA pairs for a batch of {B}")
-    i1, z1, i2, z2 = make_workload(min(B, 16), B)
+    scale, margin = args.iter_scale, args.energy_margin
+    log(f"[rank {rank}] rendering {B} distinct VGA pairs")
+    i1, z1, i2, z2, gt = render_batch(torch, B, 4_000_000 + 1000 * rank)
+    torch.cuda.synchronize()
+    valid = (z1.cpu().numpy().view(np.uint16) > 0).transpose(0, 2, 1).reshape(B, -1)
+    g = gt.cpu().numpy()
+    gt = [g[:, 0], g[:, 1], g[:, 2]]
+    d = [i1, z1, i2, z2]
+    weights = load_weights()
+    net = Net(B)
+    net.set_params(weights)
 
-    # ---------------- batched, frames resident in HBM ----------------
+    # ---------------- learned + batched, frames resident in HBM ----------------
     b = BatchSolver(ROWS, WIDTH, HEIGHT, B)
     _lib.check(lib.pdflow_set_stream(b.handle, ctypes.c_void_p(stream.cuda_stream)), "pdflow_set_stream")
-    d = [torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).to(dev) for a in (i1, z1, i2, z2)]
 
-    def step():
+    def push():
         b.push_raw_device(B, d[0].data_ptr(), d[1].data_ptr())
         b.push_raw_device(B, d[2].data_ptr(), d[3].data_ptr())
+
+    with torch.cuda.stream(stream):
+        push()
+        b.synchronize()
+        tune = autotune(lib, b.handle, B)
+        push()
         b.solve(B)
+        plain_b = b.read_flow(B)
+        e_plain = b.energy(B)
+
+    def step():
+        push()
+        return b.solve_learned(B, net, scale, margin)
 
     with torch.cuda.stream(stream):
         for _ in range(W):
             step()
     b.synchronize()
-    cfg_launch = ctypes.c_uint()
-    _lib.check(lib.pdflow_last_solve_launches(b.handle, ctypes.byref(cfg_launch)), "launch count")
-    pyr_levels = 6
-    launches_per_step = 2 * pyr_levels + cfg_launch.value      # 2 pushes x (decode + 5 pyramid levels) + solve
+    cnt = ctypes.c_uint()
+    _lib.check(lib.pdflow_last_solve_launches(b.handle, ctypes.byref(cnt)), "launch count")
+    launches_per_step = 2 * 6 + cnt.value      # 2 pushes x (decode + 5 pyramid levels) + the learned solve
     if ws > 1:
         torch.distributed.barrier()
     sampler = ClockSampler(local)
@@ -239,11 +314,12 @@ def ours(args):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     t_all0, t_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    fallbacks = 0
     with torch.cuda.stream(stream):
         t_all0.record(stream)
         for k in range(K):
             ev[k][0].record(stream)
-            step()
+            fallbacks += step()["fallbacks"]
             ev[k][1].record(stream)
         t_all1.record(stream)
     b.synchronize()
@@ -256,6 +332,30 @@ def ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     value = ws * B * K / (total_ms / 1000.0)
+    learned = b.read_flow(B)
+    e_learned = b.energy(B)
+    ep_plain = epe(learned, plain_b, valid)
+    accuracy = {"iter_scale": scale, "energy_margin": margin, "fallbacks_per_step": fallbacks / K,
+                "epe_vs_plain_mm": float(ep_plain.mean() * 1e3), "epe_vs_plain_max_pair_mm": float(ep_plain.max() * 1e3),
+                "epe_bar_mm": 1.0, "epe_bar_met": bool(ep_plain.mean() <= 1e-3),
+                "epe_vs_ground_truth_mm": {"learned": float(epe(learned, gt, valid).mean() * 1e3),
+                                           "plain": float(epe(plain_b, gt, valid).mean() * 1e3)},
+                "energy_ratio_to_plain": float((e_learned / e_plain).mean())}
+
+    # plain batched on the same handle (the schedule without the network)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            push()
+            b.solve(B)
+        b.synchronize()
+        ta, tb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ta.record(stream)
+        for _ in range(max(3, K // 2)):
+            push()
+            b.solve(B)
+        tb.record(stream)
+    torch.cuda.synchronize()
+    batched_plain = {"pairs_s": B * max(3, K // 2) / (ta.elapsed_time(tb) / 1000.0), "epe_vs_plain_mm": 0.0}
 
     # ---------------- roofline: the finest level's iterations ----------------
     hbm_peak, peak_kind = measured_peaks()
@@ -276,21 +376,25 @@ def ours(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": traffic, "traffic_basis": "DRAM bytes per iteration of the timed level (scaled ncu capture)",
                 "peak_kind": peak_kind,
-                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles, <=4 iterations per launch)",
+                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles, autotuned iterations per "
+                          "launch)",
                 "algorithmic_bytes_per_px_iter": ALG_BYTES_PER_PX_ITER,
                 "ms_per_iteration": ms.value / iters}
 
     # ---------------- e2e through the public API, host buffers ----------------
-    h = [torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a).pin_memory() for a in (i1, z1, i2, z2)]
+    h = [x.cpu().pin_memory() for x in d]
     N = ROWS * (ROWS * 4 // 3)
     hout = [torch.empty((B, N), dtype=torch.float32).pin_memory() for _ in range(3)]
+    opts = _lib.LearnedOpts(scale, margin)
+    rep = _lib.LearnedReport()
 
     def e2e_step():
         _lib.check(lib.pdflow_push_frames_u16(b.handle, B, ctypes.c_void_p(h[0].data_ptr()),
                                               ctypes.c_void_p(h[1].data_ptr())), "push")
         _lib.check(lib.pdflow_push_frames_u16(b.handle, B, ctypes.c_void_p(h[2].data_ptr()),
                                               ctypes.c_void_p(h[3].data_ptr())), "push")
-        _lib.check(lib.pdflow_solve_batch(b.handle, B), "solve")
+        _lib.check(lib.pdflow_solve_batch_learned(b.handle, B, net.handle, ctypes.byref(opts), ctypes.byref(rep)),
+                   "solve")
         _lib.check(lib.pdflow_read_flow_batch(b.handle, B, *[ctypes.c_void_p(x.data_ptr()) for x in hout]), "read")
 
     for _ in range(min(W, 2)):
@@ -308,8 +412,8 @@ def ours(args):
     e2e_ms = t0.elapsed_time(t1)
     e2e = {"value": ws * B * ke / (e2e_ms / 1000.0), "unit": "pairs/s",
            "h2d_bytes_per_step": int(2 * B * WIDTH * HEIGHT * 3), "d2h_bytes_per_step": int(3 * B * N * 4)}
-    # parity spot check of the batch against a single-pair solve of pair 0
     b.close()
+    net.close()
 
     # ---------------- plain single-pair solver ----------------
     s = Solver(ROWS, WIDTH, HEIGHT).initializeCUDA()
@@ -342,17 +446,29 @@ def ours(args):
     plain = {"pairs_s": 1000.0 / statistics.mean(single_ms), "p50_ms": statistics.median(single_ms),
              "p99_ms": float(np.quantile(single_ms, 0.99)), "steps": ns, "l2": "256 MB flush before each step"}
 
+    serving = None
+    if rank == 0 and args.serve_seconds > 0:
+        try:
+            serving = serving_run(torch, weights, scale, margin, seconds=args.serve_seconds)
+        except Exception as ex:
+            serving = {"error": str(ex)}
+
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"VGA scene flow, rows=480 (640x480, 6 levels, 25..100 iterations), "
-                                   f"batch of {B} pairs per step", "rows": ROWS, "image": f"{WIDTH}x{HEIGHT}",
-                       "pairs_per_step_per_gpu": B, "parallelism": f"replicas x{ws}", "learned_warm_start": False,
+            "config": {"workload": f"VGA scene flow, rows=480 (640x480, 6 levels), learned warm start at 60x80 "
+                                   f"with {scale:g}x iterations and 1 % energy fallback, batch of {B} distinct pairs "
+                                   "per step", "rows": ROWS, "image": f"{WIDTH}x{HEIGHT}",
+                       "pairs_per_step_per_gpu": B, "parallelism": f"replicas x{ws}", "learned_warm_start": True,
                        "l2": "batch working set far above L2 (no flush); plain single pair: L2 flushed per step",
-                       "distinct_scenes": min(B, 16)},
+                       "scenes": "seeded plane + 1-8 rigidly moving boxes/spheres, rendered on the GPU"},
+            "accuracy": accuracy,
             "batched": {"pairs_s": value, "p50_ms_per_batch": statistics.median(step_ms),
                         "p99_ms_per_batch": float(np.quantile(step_ms, 0.99))},
-            "plain": plain, "p99_ms": plain["p99_ms"], "e2e": e2e, "roofline": roofline,
+            "batched_plain": batched_plain, "plain": plain,
+            "speedup_vs_plain_single": value / plain["pairs_s"],
+            "p99_ms": serving["vga_p99_ms"] if serving and "vga_p99_ms" in serving else None,
+            "serving": serving, "autotune": tune, "e2e": e2e, "roofline": roofline,
             "gpu_launches": launches_per_step * K, "clocks": clocks}
     if rank == 0:
         try:
@@ -364,6 +480,24 @@ def ours(args):
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def autotune(lib, handle, n):
+    """Per-level launch forms for this batch (pdflow_autotune)."""
+
+    class Level(ctypes.Structure):
+        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 5)]
+
+    class Report(ctypes.Structure):
+        _fields_ = [("levels", ctypes.c_uint), ("level", Level * 8)]
+
+    rep = Report()
+    lib.pdflow_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(Report)]
+    from pdflow import _lib
+    _lib.check(lib.pdflow_autotune(handle, n, 6, ctypes.byref(rep)), "pdflow_autotune")
+    return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
+             "ms_per_iter": [None if not np.isfinite(x) else round(float(x), 4) for x in rep.level[i].ms_per_iter]}
+            for i in range(rep.levels)]
 
 
 def reference_cuda_timing():
@@ -395,6 +529,9 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--iter-scale", type=float, default=0.75)
+    ap.add_argument("--energy-margin", type=float, default=0.01)
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
