@@ -201,6 +201,19 @@ def profiled_traffic():
     return None
 
 
+def replica_value(torch, total_ms: float, pairs_per_rank: int, steps: int, device=None):
+    """Whole-job pairs/s of N independent replicas: every rank solved
+    pairs_per_rank pairs per step for `steps` steps; the job took the slowest
+    rank's time (max over ranks).  Returns (pairs/s, max elapsed ms)."""
+    import torch.distributed as dist
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    slowest = float(t.item())
+    return ws * pairs_per_rank * steps / (slowest / 1000.0), slowest
+
+
 def render_batch(torch, B, seed0=4_000_000):
     """B distinct seeded VGA pairs (1-8 objects) rendered on the GPU, with the
     ground-truth motion of frame 1."""
@@ -326,12 +339,7 @@ def ours(args):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(e) for a, e in ev]
-    total_ms = t_all0.elapsed_time(t_all1)
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = ws * B * K / (total_ms / 1000.0)
+    value, total_ms = replica_value(torch, t_all0.elapsed_time(t_all1), B, K, device=dev)
     learned = b.read_flow(B)
     e_learned = b.energy(B)
     ep_plain = epe(learned, plain_b, valid)
@@ -486,7 +494,7 @@ def autotune(lib, handle, n):
     """Per-level launch forms for this batch (pdflow_autotune)."""
 
     class Level(ctypes.Structure):
-        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 5)]
+        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 11)]
 
     class Report(ctypes.Structure):
         _fields_ = [("levels", ctypes.c_uint), ("level", Level * 8)]

@@ -104,6 +104,13 @@ int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, con
 int pdflow_read_level_images(pdflow_solver* s, unsigned level, int frame, float* colour, float* depth, float* xx,
                              float* yy);
 
+/* CSF_cuda::copyAllSolutions (pdflow_cudalib.cu:224-237): the motion field
+ * and both frames' depth, intensity and back-projected xx, yy at the finest
+ * solved level (rows*cols floats each, column-major; the point cloud the
+ * reference's live viewer draws).  Any pointer may be NULL; blocks. */
+int pdflow_read_all_solutions(pdflow_solver* s, float* dx, float* dy, float* dz, float* depth, float* depth_old,
+                              float* colour, float* colour_old, float* xx, float* xx_old, float* yy, float* yy_old);
+
 /* Waits for all work queued on the solver's stream. */
 int pdflow_synchronize(pdflow_solver* s);
 
@@ -176,12 +183,14 @@ int pdflow_read_flow_slots(pdflow_solver* s, unsigned n, const unsigned* slots, 
  * A level's iterations can run as two kernels per iteration (form 0), one
  * persistent launch per level (form 1: one CTA, a cluster, or, for a single
  * pair, the cooperative grid) or temporally blocked shared-memory tiles with
- * 2..4 iterations per launch (form 2; the iterations between two grid-wide
- * synchronisations).  pdflow_autotune times every eligible candidate of every
+ * 2..4 iterations per launch (the iterations between two grid-wide
+ * synchronisations), one pixel per lane (form 2) or pixel pairs in packed
+ * FP32x2 arithmetic (form 3: 40x40 tiles, 576 threads; form 4: 40x34 tiles,
+ * 1008 threads).  pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 8) and keeps the fastest per level; all forms give the same bits.  The
  * handle's solution state is overwritten (the pushed frames are kept). */
-#define PDFLOW_TUNE_CANDIDATES 5      /* form 0, form 1, form 2 x {2, 3, 4} iterations per launch */
+#define PDFLOW_TUNE_CANDIDATES 11     /* form 0, form 1, forms 2, 3, 4 x {2, 3, 4} iterations per launch */
 typedef struct pdflow_tune_level {
     int form;                         /* chosen form */
     unsigned iters_per_launch;        /* chosen iterations per launch (form 2) */

@@ -88,6 +88,16 @@ public:
         check(pdflow_read_flow(handle_, dxp.data(), dyp.data(), dzp.data()), "pdflow_read_flow");
     }
 
+    // CSF_cuda::copyAllSolutions: the motion field and both frames' images at
+    // the finest solved level (rows*cols floats each); any pointer may be null.
+    void copyAllSolutions(float* dx, float* dy, float* dz, float* depth, float* depth_old, float* colour,
+                          float* colour_old, float* xx, float* xx_old, float* yy, float* yy_old)
+    {
+        check(pdflow_read_all_solutions(handle_, dx, dy, dz, depth, depth_old, colour, colour_old, xx, xx_old, yy,
+                                        yy_old),
+              "pdflow_read_all_solutions");
+    }
+
     void freeGPUMemory()
     {
         if (handle_) pdflow_destroy(handle_);

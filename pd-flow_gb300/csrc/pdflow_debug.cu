@@ -56,6 +56,27 @@ int pdflow_read_level_images(pdflow_solver* s, unsigned level, int frame, float*
     return e == cudaSuccess ? PDFLOW_OK : fail("synchronize", e);
 }
 
+int pdflow_read_all_solutions(pdflow_solver* s, float* dx, float* dy, float* dz, float* depth, float* depth_old,
+                              float* colour, float* colour_old, float* xx, float* xx_old, float* yy, float* yy_old)
+{
+    if (!s) return fail(PDFLOW_ERR_ARG, "null handle");
+    unsigned li = 0;
+    level_geom(s, s->ctf_levels - 1, &li);   // the image level of the finest solved level
+    int rc = pdflow_read_level_images(s, li, 1, colour, depth, xx, yy);
+    if (!rc) rc = pdflow_read_level_images(s, li, 0, colour_old, depth_old, xx_old, yy_old);
+    if (rc) return rc;
+    if (!dx && !dy && !dz) return PDFLOW_OK;
+    const size_t n = size_t(s->rows) * s->cols * 4;
+    float* dst[3] = {dx, dy, dz};
+    const float* src[3] = {s->dx, s->dy, s->dz};
+    for (int a = 0; a < 3; ++a)
+        if (dst[a]) {
+            cudaError_t e = cudaMemcpyAsync(dst[a], src[a], n, cudaMemcpyDeviceToHost, s->stream);
+            if (e != cudaSuccess) return fail("motion field copy", e);
+        }
+    return check_status(s);
+}
+
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 {
     if (!s || !fn) return PDFLOW_ERR_ARG;
@@ -112,7 +133,7 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 
 int pdflow_set_iteration_form(pdflow_solver* s, int form)
 {
-    if (!s || form < 0 || form > 2) return PDFLOW_ERR_ARG;
+    if (!s || form < 0 || form > 4) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..4");
     if (s->iter_form != form) {
         cudaStreamSynchronize(s->stream);
         s->iter_form = form;   // graphs are cached per iteration form

@@ -32,7 +32,8 @@ struct pdflow_solver {
     unsigned* flags = nullptr;           // per-CTA progress counters of the grid-form iteration
     unsigned* status = nullptr;          // device status word (0 = ok)
     int num_sms = 0;
-    int iter_form = 2;                   // 2 = tiles for large levels, 1 = one launch per level, 0 = two kernels per iteration
+    int iter_form = 4;                   // 4 / 3 / 2 = narrow paired / paired / scalar tiles for large levels,
+                                         // 1 = one launch per level, 0 = two kernels per iteration
     int level_form[8] = {-1, -1, -1, -1, -1, -1, -1, -1};   // per-level override (autotuner); -1 = iter_form's choice
     unsigned level_kk[8] = {};           // tile form: iterations per launch (0 = the halo width)
     float* dx = nullptr;

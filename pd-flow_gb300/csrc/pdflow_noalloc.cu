@@ -86,6 +86,7 @@ int setup_device(int dev, void** scratch, int* num_sms)
     if (!(prop.major == 10 && prop.minor == 3)) return fail(PDFLOW_ERR_NO_DEVICE, "needs an sm_103 (GB300) device");
     e = pdflow::prepare_iterate();
     if (e == cudaSuccess) e = pdflow::prepare_tiles();
+    if (e == cudaSuccess) e = pdflow::prepare_tiles2();
     if (e != cudaSuccess) return fail(PDFLOW_ERR_CUDA, "kernel attributes", e);
     void* addr = nullptr;
     e = cudaGetSymbolAddress(&addr, g_scratch);

@@ -190,13 +190,15 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
     const int forced = level < 8 ? s->level_form[level] : -1;
     const bool one_launch_ok = (pairs == 1 || pl.mode != kIterGrid) && pl.smem_bytes <= iterate_smem_limit();
     bool tiles, one_launch;
+    const int form = forced >= 0 ? forced : s->iter_form;
     if (forced >= 0) {
-        tiles = forced == 2 && iters > 0;
+        tiles = forced >= 2 && iters > 0;
         one_launch = forced == 1 && iters > 0 && one_launch_ok;
     } else {
-        tiles = s->iter_form == 2 && iters > 0 && pl.mode == kIterGrid && pairs > 1;
+        tiles = s->iter_form >= 2 && iters > 0 && pl.mode == kIterGrid && pairs > 1;
         one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
     }
+    const bool paired = tiles && form >= 3, narrow = form == 4;
     if (tiles) {
         State cur = s->S;
         State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
@@ -206,8 +208,12 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
                                : tiles_halo();
         for (unsigned done = 0; done < iters;) {
             const unsigned kk = (iters - done < h) ? iters - done : h;
-            CUDA_TRY(launch_iterate_tiles(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st),
-                     "tile iteration launch");
+            if (paired)
+                CUDA_TRY(launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, narrow),
+                         "tile iteration launch");
+            else
+                CUDA_TRY(launch_iterate_tiles(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st),
+                         "tile iteration launch");
             const State t = cur;
             cur = nxt;
             nxt = t;
@@ -437,6 +443,7 @@ int pdflow_create_batch(unsigned rows, unsigned width, unsigned height, const pd
         if (!prepared) {
             CUDA_TRY(prepare_iterate(), "kernel attributes");
             CUDA_TRY(prepare_tiles(), "kernel attributes");
+            CUDA_TRY(prepare_tiles2(), "kernel attributes");
             prepared = true;
         }
     }

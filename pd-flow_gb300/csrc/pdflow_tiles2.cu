@@ -1,0 +1,409 @@
+// Temporally blocked primal-dual iterations, paired form.
+//
+// Same tiling as pdflow_tiles.cu (40x40 interior, 4-pixel halo, 48x48 region
+// of 24 planes in shared memory, kk <= 4 iterations per launch, alternating
+// state buffers), but each of the 576 threads owns two vertically adjacent
+// pixel pairs (v, v+1) in each of two region columns (or, in the narrow
+// shape, 40x34 interiors and 1008 threads owning one pair each).  A pair's arithmetic
+// runs as packed FP32x2 instructions (fma/add/sub/mul.rn.f32x2: each lane
+// rounds exactly as the scalar __f*_rn operation, so the results are the
+// same bits as the scalar kernels, as long as no packed product feeds only a
+// packed sum, see the dw update), its own and horizontally neighbouring
+// values are read with 8-byte shared loads, and only the vertical neighbour
+// beyond the pair needs a scalar load.  Work that depends on a lane's branch
+// (clamping, disc projection with rhypotf, the shrinkage cases) stays scalar.
+//
+// Every valid pixel of the region is updated in every iteration: pixels in the
+// stale ring at a non-border region edge compute garbage from stale
+// neighbours, exactly as they would hold stale values if skipped, and no exact
+// pixel ever reads them.  Reads beyond a region edge are redirected into the
+// region's own storage, so every shared access stays in bounds.
+#include "pdflow_iterate.cuh"
+#include "pdflow_math.cuh"
+
+namespace pdflow {
+
+namespace {
+
+constexpr int kTV = 40, kH = 4;
+constexpr int kRV = kTV + 2 * kH;                       // 48 region rows
+constexpr int kPV = kRV / 2;                            // pixel pairs per region column
+
+// Two shapes: TU = 40 interior columns with 576 threads owning two pairs each,
+// or TU = 34 with 1008 threads owning one pair each (more warps per SM,
+// slightly more halo).
+template <int TU>
+struct Shape {
+    static constexpr int kTU = TU, kRU = TU + 2 * kH, kPlane = kRV * kRU;
+    static constexpr int kCols = TU == 40 ? 2 : 1;      // region columns per thread
+    static constexpr int kTY = kRU / kCols;             // columns per sweep
+    static constexpr int kThreads = kPV * kTY;
+    static_assert(kTY * kCols == kRU && kThreads <= 1024, "paired tile layout");
+};
+
+enum { T_DU, T_DV, T_DW, T_UA, T_VA, T_WA, T_PD, T_PUU, T_PUV, T_PVU, T_PVV, T_PWU, T_PWV,
+       T_MU, T_DDT, T_DDU, T_DDV, T_DCT, T_DCU, T_DCV, T_RI, T_RJ, T_DUP, T_DVP, T_NPLANES };
+
+struct Tile2Args {
+    LevelGeom g;
+    LevelConsts L;
+    State src, dst;
+    Params p;
+    const float* depth_old;
+    unsigned kk;
+    bool last;
+    unsigned tiles_v;
+};
+
+// ---- packed FP32x2 arithmetic (per-lane IEEE round-to-nearest) ----
+__device__ __forceinline__ unsigned long long pk(float2 a)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 upk(unsigned long long v)
+{
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ float2 fm2(float2 a, float2 b, float2 c)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pk(a)), "l"(pk(b)), "l"(pk(c)));
+    return upk(r);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk(a)), "l"(pk(b)));
+    return upk(r);
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk(a)), "l"(pk(b)));
+    return upk(r);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk(a)), "l"(pk(b)));
+    return upk(r);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+
+// pair flags
+enum : unsigned { F_V0 = 1, F_V1 = 2, F_FU = 4, F_LU = 8, F_FV0 = 16, F_LV0 = 32, F_LV1 = 64 };
+
+__device__ __forceinline__ void clamp_pd(float& pd)
+{
+    if (fabsf(pd) > 1.f) pd = (pd > 1.f) ? 1.f : -1.f;
+}
+
+template <int TU>
+__global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2Args a)
+{
+    using S = Shape<TU>;
+    constexpr int kTU = S::kTU, kRU = S::kRU, kPlane = S::kPlane, kCols = S::kCols, kTY = S::kTY;
+    extern __shared__ __align__(16) float sm[];
+    const size_t po = pair_off(a.g.map, a.g.pstride, blockIdx.y);
+    const LevelConsts L = at(a.L, po);
+    const State src = at(a.src, po), dst = at(a.dst, po);
+    const float* depth_old = at(a.depth_old, po);
+    const int R = (int)a.g.R, C = (int)a.g.C;
+    const int tv = (int)(blockIdx.x % a.tiles_v), tu = (int)(blockIdx.x / a.tiles_v);
+    const int iv0 = tv * kTV, iu0 = tu * kTU;
+    const int iv1 = min(iv0 + kTV, R), iu1 = min(iu0 + kTU, C);
+    const int rv0 = max(iv0 - kH, 0), ru0 = max(iu0 - kH, 0);
+    const int rv1 = min(iv1 + kH, R), ru1 = min(iu1 + kH, C);
+    const int RV = rv1 - rv0, RU = ru1 - ru0;
+    const int tx = threadIdx.x % kPV, ty = threadIdx.x / kPV;
+    const int rv = 2 * tx;                      // the pair's first row in the region
+    const bool even_rows = (R & 1) == 0;        // global pair loads are 8-byte aligned
+    float* P[T_NPLANES];
+#pragma unroll
+    for (int k = 0; k < T_NPLANES; ++k) P[k] = sm + k * kPlane;
+
+    // ---- load the region ----
+    {
+        const float* gs[T_NPLANES] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd, src.puu, src.puv,
+                                      src.pvu, src.pvv, src.pwu, src.pwv, L.mu, L.ddt, L.ddu, L.ddv, L.dct, L.dcu,
+                                      L.dcv, L.ri, L.rj, L.du_prev, L.dv_prev};
+#pragma unroll
+        for (int c = 0; c < kCols; ++c) {
+            const int ru = ty + kTY * c;
+            if (ru >= RU || rv >= RV) continue;
+            const int q = rv + ru * kRV;
+            const size_t gi = (size_t)(rv0 + rv) + (size_t)(ru0 + ru) * R;
+            if (even_rows) {
+#pragma unroll
+                for (int k = 0; k < T_NPLANES; ++k) st2(P[k] + q, __ldg(reinterpret_cast<const float2*>(gs[k] + gi)));
+            } else {
+                const bool v1 = rv + 1 < RV;
+#pragma unroll
+                for (int k = 0; k < T_NPLANES; ++k) {
+                    P[k][q] = __ldg(gs[k] + gi);
+                    if (v1) P[k][q + 1] = __ldg(gs[k] + gi + 1);
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    const float li = a.p.lambda_i, ld = a.p.lambda_d;
+    unsigned flags[kCols];
+    float2 sg[kCols][8];   // spd*mu, spuvx*li, spuvy*li, spwx*ld, spwy*ld, tau_u, tau_v, tau_w
+#pragma unroll
+    for (int c = 0; c < kCols; ++c) {
+        const int ru = ty + kTY * c;
+        const int u = ru0 + ru, v0 = rv0 + rv;
+        unsigned f = 0;
+        if (ru < RU) {
+            if (rv < RV) f |= F_V0;
+            if (rv + 1 < RV) f |= F_V1;
+        }
+        if (u == 0) f |= F_FU;
+        if (u == C - 1) f |= F_LU;
+        if (v0 == 0) f |= F_FV0;
+        if (v0 == R - 1) f |= F_LV0;
+        if (v0 + 1 == R - 1) f |= F_LV1;
+        flags[c] = f;
+        const int q = rv + ru * kRV;
+        float s[2][8];
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const bool valid = l == 0 ? (f & F_V0) : (f & F_V1);
+            if (!valid) {
+#pragma unroll
+                for (int m = 0; m < 8; ++m) s[l][m] = 0.f;
+                continue;
+            }
+            const int ql = q + l, rvl = rv + l;
+            const bool fu = f & F_FU, fv = (l == 0) && (f & F_FV0);
+            const float mu = P[T_MU][ql], ddu = P[T_DDU][ql], ddv = P[T_DDV][ql], ri = P[T_RI][ql], rj = P[T_RJ][ql];
+            // the set-up kernel's expressions (mu_and_steps); at a region edge that is not an
+            // image border the left/top neighbour is missing: that pixel is stale anyway
+            const float ri_m = (fu || ru == 0) ? ri : P[T_RI][ql - kRV];
+            const float rj_m = (fv || rvl == 0) ? rj : P[T_RJ][ql - 1];
+            const float spd = fdividef(1.f, fm(mu, add(add(1.f, fabsf(ddu)), fabsf(ddv)), 1e-10f));
+            s[l][0] = mul(spd, mu);
+            s[l][1] = mul(fdividef(0.5f, fm(li, ri, 1e-10f)), li);
+            s[l][2] = mul(fdividef(0.5f, fm(li, rj, 1e-10f)), li);
+            s[l][3] = mul(fdividef(0.5f, fm(ri, ld, 1e-10f)), ld);
+            s[l][4] = mul(fdividef(0.5f, fm(rj, ld, 1e-10f)), ld);
+            float acu_r = add(ri, rj);
+            if (!fu) acu_r = add(acu_r, ri_m);
+            if (!fv) acu_r = add(acu_r, rj_m);
+            s[l][5] = fdividef(1.f, add(fm(li, acu_r, mul(mu, fabsf(ddu))), 1e-10f));
+            s[l][6] = fdividef(1.f, add(fm(li, acu_r, mul(mu, fabsf(ddv))), 1e-10f));
+            s[l][7] = fdividef(1.f, add(fm(ld, acu_r, mu), 1e-10f));
+        }
+#pragma unroll
+        for (int m = 0; m < 8; ++m) sg[c][m] = make_float2(s[0][m], s[1][m]);
+    }
+    const float2 li2 = make_float2(li, li), ld2v = make_float2(ld, ld), two = make_float2(2.f, 2.f);
+    const float2 zero = make_float2(0.f, 0.f);
+
+    for (unsigned j = 0; j < a.kk; ++j) {
+        const bool last_iter = a.last && (j + 1 == a.kk);
+        // ---- dual step (in place: each pixel reads only its own duals) ----
+#pragma unroll
+        for (int c = 0; c < kCols; ++c) {
+            const unsigned f = flags[c];
+            if (!(f & F_V0)) continue;
+            const int ru = ty + kTY * c, q = rv + ru * kRV;
+            const int qu = (ru + 1 < kRU) ? q + kRV : q;           // beyond the region: own storage
+            const int qv = (rv + 2 < kRV) ? q + 2 : q + 1;
+            const float2 ua = ld2(P[T_UA] + q), va = ld2(P[T_VA] + q), wa = ld2(P[T_WA] + q);
+            const float2 dup = ld2(P[T_DUP] + q), dvp = ld2(P[T_DVP] + q);
+            const float2 ri = ld2(P[T_RI] + q), rj = ld2(P[T_RJ] + q);
+            float2 gu1 = zero, gv1 = zero, gw1 = zero;
+            if (!(f & F_LU)) {
+                const float2 ua1 = ld2(P[T_UA] + qu), va1 = ld2(P[T_VA] + qu), wa1 = ld2(P[T_WA] + qu);
+                const float2 dup1 = ld2(P[T_DUP] + qu), dvp1 = ld2(P[T_DVP] + qu);
+                gu1 = mul2(ri, sub2(add2(ua1, dup1), add2(ua, dup)));
+                gv1 = mul2(ri, sub2(add2(va1, dvp1), add2(va, dvp)));
+                gw1 = mul2(ri, sub2(wa1, wa));
+            }
+            const float2 uav = make_float2(ua.y, P[T_UA][qv]), vav = make_float2(va.y, P[T_VA][qv]);
+            const float2 wav = make_float2(wa.y, P[T_WA][qv]);
+            const float2 dupv = make_float2(dup.y, P[T_DUP][qv]), dvpv = make_float2(dvp.y, P[T_DVP][qv]);
+            float2 gu2 = mul2(rj, sub2(add2(uav, dupv), add2(ua, dup)));
+            float2 gv2 = mul2(rj, sub2(add2(vav, dvpv), add2(va, dvp)));
+            float2 gw2 = mul2(rj, sub2(wav, wa));
+            if (f & F_LV0) { gu2.x = 0.f; gv2.x = 0.f; gw2.x = 0.f; }
+            if (f & F_LV1) { gu2.y = 0.f; gv2.y = 0.f; gw2.y = 0.f; }
+            const float2 X = fm2(ld2(P[T_DDV] + q), va, fm2(ld2(P[T_DDU] + q), ua, sub2(ld2(P[T_DDT] + q), wa)));
+            float2 pd = fm2(sg[c][0], X, ld2(P[T_PD] + q));
+            float2 puu = fm2(sg[c][1], gu1, ld2(P[T_PUU] + q)), puv = fm2(sg[c][2], gu2, ld2(P[T_PUV] + q));
+            float2 pvu = fm2(sg[c][1], gv1, ld2(P[T_PVU] + q)), pvv = fm2(sg[c][2], gv2, ld2(P[T_PVV] + q));
+            float2 pwu = fm2(sg[c][3], gw1, ld2(P[T_PWU] + q)), pwv = fm2(sg[c][4], gw2, ld2(P[T_PWV] + q));
+            clamp_pd(pd.x);
+            clamp_pd(pd.y);
+            project_disc(puu.x, puv.x);
+            project_disc(puu.y, puv.y);
+            project_disc(pvu.x, pvv.x);
+            project_disc(pvu.y, pvv.y);
+            project_disc(pwu.x, pwv.x);
+            project_disc(pwu.y, pwv.y);
+            st2(P[T_PD] + q, pd);
+            st2(P[T_PUU] + q, puu);
+            st2(P[T_PUV] + q, puv);
+            st2(P[T_PVU] + q, pvu);
+            st2(P[T_PVV] + q, pvv);
+            st2(P[T_PWU] + q, pwu);
+            st2(P[T_PWV] + q, pwv);
+        }
+        __syncthreads();
+        // ---- primal step (in place: each pixel writes only its own primal) ----
+#pragma unroll
+        for (int c = 0; c < kCols; ++c) {
+            const unsigned f = flags[c];
+            if (!(f & F_V0)) continue;
+            const int ru = ty + kTY * c, q = rv + ru * kRV;
+            const int qm = ru > 0 ? q - kRV : q;                   // beyond the region: own storage
+            const int qvm = rv > 0 ? q - 1 : q;
+            const bool fu = f & F_FU, lu = f & F_LU;
+            const float2 ri = ld2(P[T_RI] + q), rj = ld2(P[T_RJ] + q);
+            const float2 rim = ld2(P[T_RI] + qm);
+            const float2 rjm = make_float2(P[T_RJ][qvm], rj.x);
+            const float2 puu = ld2(P[T_PUU] + q), puv = ld2(P[T_PUV] + q);
+            const float2 pvu = ld2(P[T_PVU] + q), pvv = ld2(P[T_PVV] + q);
+            const float2 pwu = ld2(P[T_PWU] + q), pwv = ld2(P[T_PWV] + q);
+            const float2 puum = ld2(P[T_PUU] + qm), pvum = ld2(P[T_PVU] + qm), pwum = ld2(P[T_PWU] + qm);
+            const float2 puvm = make_float2(P[T_PUV][qvm], puv.x), pvvm = make_float2(P[T_PVV][qvm], pvv.x);
+            const float2 pwvm = make_float2(P[T_PWV][qvm], pwv.x);
+            float2 div[3];
+            const float2 pu_[3] = {puu, pvu, pwu}, pv_[3] = {puv, pvv, pwv};
+            const float2 pum_[3] = {puum, pvum, pwum}, pvm_[3] = {puvm, pvvm, pwvm};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float2 d;
+                if (fu) d = mul2(ri, pu_[k]);
+                else if (lu) d = mul2(neg2(rim), pum_[k]);
+                else d = fm2(ri, pu_[k], neg2(mul2(rim, pum_[k])));
+                float2 g = add2(d, fm2(rj, pv_[k], neg2(mul2(rjm, pvm_[k]))));
+                if (f & F_FV0) g.x = fm(rj.x, pv_[k].x, d.x);
+                else if (f & F_LV0) g.x = fm(-rjm.x, pvm_[k].x, d.x);
+                if (f & F_LV1) g.y = fm(-rjm.y, pvm_[k].y, d.y);
+                div[k] = g;
+            }
+            const float2 mu = ld2(P[T_MU] + q), pd = ld2(P[T_PD] + q);
+            const float2 dcu = ld2(P[T_DCU] + q), dcv = ld2(P[T_DCV] + q), dct = ld2(P[T_DCT] + q);
+            float2 du = ld2(P[T_DU] + q), dv = ld2(P[T_DV] + q), dw = ld2(P[T_DW] + q);
+            const float2 du_old = du, dv_old = dv, dw_old = dw;
+            const float2 tu = sg[c][5], tv = sg[c][6], tw = sg[c][7];
+            du = fm2(neg2(tu), fm2(mul2(mu, ld2(P[T_DDU] + q)), pd, neg2(mul2(li2, div[0]))), du);
+            dv = fm2(neg2(tv), fm2(mul2(mu, ld2(P[T_DDV] + q)), pd, neg2(mul2(li2, div[1]))), dv);
+            // Per lane: a packed multiply whose only use is a packed add may be contracted
+            // into one fused multiply-add by the assembler, which changes the rounding of
+            // add(dw, mul(-tw, .)); the scalar intrinsics are never contracted.
+            {
+                const float2 t = fm2(neg2(mu), pd, neg2(mul2(ld2v, div[2])));
+                dw.x = add(dw.x, mul(-tw.x, t.x));
+                dw.y = add(dw.y, mul(-tw.y, t.y));
+            }
+            const float2 of = fm2(dcv, dv, fm2(dcu, du, dct));
+            const float2 a1 = mul2(tu, dcu), b1 = mul2(tv, dcv);
+            const float2 th = fm2(a1, dcu, mul2(b1, dcv));
+            // L1 shrinkage, per lane (pdflow_cudalib.cu:906-923)
+            {
+                if (of.x < -th.x) { du.x = add(du.x, a1.x); dv.x = add(dv.x, b1.x); }
+                else if (of.x > th.x) { du.x = sub(du.x, a1.x); dv.x = sub(dv.x, b1.x); }
+                else {
+                    const float den = add(th.x, 1e-10f);
+                    du.x = sub(du.x, qt(mul(a1.x, of.x), den));
+                    dv.x = sub(dv.x, qt(mul(b1.x, of.x), den));
+                }
+                if (of.y < -th.y) { du.y = add(du.y, a1.y); dv.y = add(dv.y, b1.y); }
+                else if (of.y > th.y) { du.y = sub(du.y, a1.y); dv.y = sub(dv.y, b1.y); }
+                else {
+                    const float den = add(th.y, 1e-10f);
+                    du.y = sub(du.y, qt(mul(a1.y, of.y), den));
+                    dv.y = sub(dv.y, qt(mul(b1.y, of.y), den));
+                }
+            }
+            const float2 nua = fm2(two, du, neg2(du_old)), nva = fm2(two, dv, neg2(dv_old));
+            const float2 nwa = fm2(two, dw, neg2(dw_old));
+            if (last_iter) {
+                const size_t gi = (size_t)(rv0 + rv) + (size_t)(ru0 + ru) * R;
+                const float2 dup = ld2(P[T_DUP] + q), dvp = ld2(P[T_DVP] + q);
+                saturate(du.x, dv.x, dw.x, dup.x, dvp.x, __ldg(depth_old + gi));
+                if (f & F_V1) saturate(du.y, dv.y, dw.y, dup.y, dvp.y, __ldg(depth_old + gi + 1));
+            }
+            st2(P[T_DU] + q, du);
+            st2(P[T_DV] + q, dv);
+            st2(P[T_DW] + q, dw);
+            st2(P[T_UA] + q, nua);
+            st2(P[T_VA] + q, nva);
+            st2(P[T_WA] + q, nwa);
+        }
+        __syncthreads();
+    }
+
+    // ---- write the interior ----
+    float* gd[13] = {dst.du, dst.dv, dst.dw, dst.dua, dst.dva, dst.dwa, dst.pd, dst.puu, dst.puv, dst.pvu, dst.pvv,
+                     dst.pwu, dst.pwv};
+    const int v0 = rv0 + rv;
+    const bool in0 = v0 >= iv0 && v0 < iv1 && rv < RV, in1 = v0 + 1 >= iv0 && v0 + 1 < iv1 && rv + 1 < RV;
+#pragma unroll
+    for (int c = 0; c < kCols; ++c) {
+        const int ru = ty + kTY * c, u = ru0 + ru;
+        if (ru >= RU || u < iu0 || u >= iu1 || !(in0 || in1)) continue;
+        const int q = rv + ru * kRV;
+        const size_t gi = (size_t)v0 + (size_t)u * R;
+        if (even_rows && in0 && in1) {
+#pragma unroll
+            for (int k = 0; k < 13; ++k) st2(gd[k] + gi, ld2(P[k] + q));
+        } else {
+#pragma unroll
+            for (int k = 0; k < 13; ++k) {
+                if (in0) gd[k][gi] = P[k][q];
+                if (in1) gd[k][gi + 1] = P[k][q + 1];
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t prepare_tiles2()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_iterate_tiles2<40>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float) * T_NPLANES * Shape<40>::kPlane));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_iterate_tiles2<34>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(float) * T_NPLANES * Shape<34>::kPlane));
+    return e;
+}
+
+template <int TU>
+static cudaError_t launch_shape(const Tile2Args& a, const LevelGeom& g, cudaStream_t st)
+{
+    using S = Shape<TU>;
+    dim3 grid(a.tiles_v * ((g.C + TU - 1) / TU), g.pairs);
+    k_iterate_tiles2<TU><<<grid, S::kThreads, sizeof(float) * T_NPLANES * S::kPlane, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
+                                  unsigned kk, bool last, cudaStream_t st, bool narrow)
+{
+    Tile2Args a;
+    a.g = g;
+    a.L = L;
+    a.src = src;
+    a.dst = dst;
+    a.p = p;
+    a.depth_old = depth_old;
+    a.kk = kk;
+    a.last = last;
+    a.tiles_v = (g.R + kTV - 1) / kTV;
+    return narrow ? launch_shape<34>(a, g, st) : launch_shape<40>(a, g, st);
+}
+
+}  // namespace pdflow

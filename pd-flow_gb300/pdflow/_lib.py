@@ -157,6 +157,8 @@ _SIGNATURES = {
     "pdflow_server_get_stats": (ctypes.c_int, [vp, ctypes.POINTER(ServerStats)]),
     "pdflow_seed_level_inputs": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_seed_level_labels": (ctypes.c_int, [vp, u32, vp]),
+    "pdflow_set_level_form": (ctypes.c_int, [vp, u32, ctypes.c_int, u32]),
+    "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
     "pdflow_gemm_bf16": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int,
                                         vp, ctypes.c_int, ctypes.c_int, vp]),
 }
@@ -286,7 +288,7 @@ class Solver(_Extras):
     freeGPUMemory."""
 
     def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 2):
+                 use_graph: bool = True, iteration_form: int = 4):
         self.rows, self.width, self.height = rows, width, height
         self.cols = rows * 320 // 240
         self.params = params
@@ -365,6 +367,15 @@ class Solver(_Extras):
               "pdflow_read_level_images")
         return dict(zip(("colour", "depth", "xx", "yy"), out))
 
+    def all_solutions(self):
+        """copyAllSolutions: dx, dy, dz and both frames' depth / colour / xx / yy
+        at the finest solved level (pdflow_read_all_solutions)."""
+        n = self.rows * self.cols
+        names = ("dx", "dy", "dz", "depth", "depth_old", "colour", "colour_old", "xx", "xx_old", "yy", "yy_old")
+        out = {k: np.zeros(n, np.float32) for k in names}
+        check(load().pdflow_read_all_solutions(self._h, *[_ptr(out[k]) for k in names]), "pdflow_read_all_solutions")
+        return out
+
     def debug_solve(self):
         store = {}
 
@@ -401,7 +412,7 @@ class BatchSolver(_Extras):
     a camera stream that keeps its previous frame on the device."""
 
     def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 2):
+                 use_graph: bool = True, iteration_form: int = 4):
         lib = load()
         self.rows, self.width, self.height, self.max_pairs = rows, width, height, max_pairs
         self.cols = rows * 320 // 240

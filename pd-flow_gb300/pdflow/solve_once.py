@@ -12,14 +12,16 @@ import argparse
 
 import numpy as np
 
-from . import BatchSolver, scenes
+from . import BatchSolver, Net, load_weights, scenes
 
 
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--rows", type=int, default=480, choices=(60, 120, 240, 480))
     ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--form", type=int, default=2, choices=(0, 1, 2))
+    ap.add_argument("--form", type=int, default=4, choices=(0, 1, 2, 3, 4))
+    ap.add_argument("--learned", type=float, default=0.0,
+                    help="iteration scale of a learned warm-started solve (0: plain solve)")
     ap.add_argument("--solves", type=int, default=2)
     ap.add_argument("--distinct", type=int, default=4)
     a = ap.parse_args()
@@ -30,10 +32,19 @@ def main() -> None:
     b = BatchSolver(a.rows, w, h, a.batch, use_graph=False, iteration_form=a.form)
     b.push_raw(stack(0), stack(1))
     b.push_raw(stack(2), stack(3))
+    net = None
+    if a.learned > 0:
+        net = Net(a.batch)
+        net.set_params(load_weights())
     for _ in range(a.solves):
-        b.solve(a.batch)
+        if net is not None:
+            b.solve_learned(a.batch, net, a.learned, 0.01)
+        else:
+            b.solve(a.batch)
     dx, dy, dz = b.read_flow(1)
     b.close()
+    if net is not None:
+        net.close()
     print(f"rows={a.rows} batch={a.batch} form={a.form}: sum|dx|+|dy|+|dz| of pair 0 = "
           f"{float(np.abs(dx).sum() + np.abs(dy).sum() + np.abs(dz).sum()):.6f}")
 

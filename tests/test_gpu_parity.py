@@ -254,3 +254,19 @@ def test_zero_iteration_schedule_still_saturates_and_filters(golden_qvga):
     for o, r in zip((s.dxp, s.dyp, s.dzp), ref):
         assert np.allclose(o, r, atol=1e-6)
     s.freeGPUMemory()
+
+
+def test_all_solutions_readback_matches_the_parts(golden_qvga):
+    """pdflow_read_all_solutions (copyAllSolutions) returns the flow and both
+    frames' images of the finest solved level."""
+    g = golden_qvga
+    s = Solver(60, 320, 240).initializeCUDA()
+    s.loadRGBDFrames(g["i1"], g["z1"], g["i2"], g["z2"])
+    s.solveSceneFlowGPU()
+    out = s.all_solutions()
+    for a, b in zip((out["dx"], out["dy"], out["dz"]), (s.dxp, s.dyp, s.dzp)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    new, old = s.level_images(2, 1), s.level_images(2, 0)      # 80x60 = rows 60 x cols 80
+    for k in ("depth", "colour", "xx", "yy"):
+        assert np.array_equal(out[k], new[k]) and np.array_equal(out[k + "_old"], old[k])
+    s.freeGPUMemory()

@@ -19,7 +19,7 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     ref = b.read_flow(3)
 
     class Level(ctypes.Structure):
-        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 5)]
+        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 11)]
 
     class Report(ctypes.Structure):
         _fields_ = [("levels", ctypes.c_uint), ("level", Level * 8)]
@@ -30,7 +30,7 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     assert lib.pdflow_autotune(b.handle, 3, 4, ctypes.byref(rep)) == 0
     assert rep.levels == 5
     for i in range(rep.levels):
-        assert rep.level[i].form in (0, 1, 2)
+        assert rep.level[i].form in (0, 1, 2, 3, 4)
         assert np.isfinite(rep.level[i].ms_per_iter[0])
     b.solve(3)
     got = b.read_flow(3)
@@ -38,9 +38,9 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
     # each tile width of iterations per launch, forced on every level
     lib.pdflow_set_level_form.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_uint]
-    for kk in (1, 2, 3):
+    for form, kk in ((2, 1), (2, 2), (2, 3), (3, 1), (3, 2), (3, 3), (3, 4), (4, 1), (4, 3), (4, 4)):
         for lvl in range(5):
-            assert lib.pdflow_set_level_form(b.handle, lvl, 2, kk) == 0
+            assert lib.pdflow_set_level_form(b.handle, lvl, form, kk) == 0
         b.solve(3)
         got = b.read_flow(3)
         for x, y in zip(got, ref):
