@@ -66,6 +66,14 @@ int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const fl
 int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned last, const float* d_seed,
                         float iter_scale, int energy_level, float* energies);
 
+/* How the paired tile kernels move a tile's region between HBM and shared
+ * memory (process-wide; graphs captured afterwards use it): shape 0 = 40x40
+ * tiles (iteration form 3), 1 = 40x34 tiles (form 4); mode bit 0 = TMA bulk
+ * copies for the region load, bit 1 = for the interior store, else plain
+ * loads/stores.  Levels whose row count is not a multiple of 4 always use
+ * plain loads and stores.  All modes give the same bits. */
+int pdflow_set_tile_copy_mode(int shape, int mode);
+
 #ifdef __cplusplus
 }
 #endif

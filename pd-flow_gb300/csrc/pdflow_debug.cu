@@ -217,4 +217,11 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
     return pdflow::check_status(s);
 }
 
+int pdflow_set_tile_copy_mode(int shape, int mode)
+{
+    if (shape < 0 || shape > 1 || mode < 0 || mode > 3) return fail(PDFLOW_ERR_ARG, "shape 0..1, mode 0..3");
+    set_tile_copy_mode(shape, mode);
+    return PDFLOW_OK;
+}
+
 }  // extern "C"

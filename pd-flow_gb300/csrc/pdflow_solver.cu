@@ -209,7 +209,8 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         for (unsigned done = 0; done < iters;) {
             const unsigned kk = (iters - done < h) ? iters - done : h;
             if (paired)
-                CUDA_TRY(launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, narrow),
+                CUDA_TRY(launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, narrow,
+                                               s->status),
                          "tile iteration launch");
             else
                 CUDA_TRY(launch_iterate_tiles(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st),

@@ -159,6 +159,7 @@ _SIGNATURES = {
     "pdflow_seed_level_labels": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_set_level_form": (ctypes.c_int, [vp, u32, ctypes.c_int, u32]),
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
+    "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "pdflow_gemm_bf16": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int,
                                         vp, ctypes.c_int, ctypes.c_int, vp]),
 }
