@@ -192,7 +192,7 @@ def profiled_traffic():
     """DRAM bytes per pixel-iteration of the tile iteration kernel, from the
     committed ncu summary (the `bytes_per_px_iter:` line), else None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "k_iterate_tiles_vga_batch16.md")) as f:
+        with open(os.path.join(ROOT, "profiles", "k_iterate_tiles2_vga_batch16.md")) as f:
             for line in f:
                 if line.startswith("bytes_per_px_iter:"):
                     return {"bytes_per_px_iter": float(line.split(":")[1])}
@@ -384,8 +384,8 @@ def ours(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": traffic, "traffic_basis": "DRAM bytes per iteration of the timed level (scaled ncu capture)",
                 "peak_kind": peak_kind,
-                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles, autotuned iterations per "
-                          "launch)",
+                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles2, autotuned form and "
+                          "iterations per launch)",
                 "algorithmic_bytes_per_px_iter": ALG_BYTES_PER_PX_ITER,
                 "ms_per_iteration": ms.value / iters}
 
@@ -502,7 +502,7 @@ def autotune(lib, handle, n):
     rep = Report()
     lib.pdflow_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(Report)]
     from pdflow import _lib
-    _lib.check(lib.pdflow_autotune(handle, n, 6, ctypes.byref(rep)), "pdflow_autotune")
+    _lib.check(lib.pdflow_autotune(handle, n, 12, ctypes.byref(rep)), "pdflow_autotune")
     return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
              "ms_per_iter": [None if not np.isfinite(x) else round(float(x), 4) for x in rep.level[i].ms_per_iter]}
             for i in range(rep.levels)]

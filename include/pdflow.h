@@ -188,7 +188,7 @@ int pdflow_read_flow_slots(pdflow_solver* s, unsigned n, const unsigned* slots, 
  * FP32x2 arithmetic (form 3: 40x40 tiles, 576 threads; form 4: 40x34 tiles,
  * 1008 threads).  pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
- * 0 = 8) and keeps the fastest per level; all forms give the same bits.  The
+ * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The
  * handle's solution state is overwritten (the pushed frames are kept). */
 #define PDFLOW_TUNE_CANDIDATES 11     /* form 0, form 1, forms 2, 3, 4 x {2, 3, 4} iterations per launch */
 typedef struct pdflow_tune_level {

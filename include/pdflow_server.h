@@ -12,6 +12,8 @@
  * (plain, or with the learned warm start); frames that arrive meanwhile wait
  * for the lane's next batch (continuous batching), and lanes run concurrently
  * on the GPU.  Per-pair results do not depend on what else is in the batch.
+ * A lane captures its CUDA graphs for every batch size when it is created
+ * (on blank frames), so admission, not a live request, pays for them.
  */
 #ifndef PDFLOW_SERVER_H
 #define PDFLOW_SERVER_H

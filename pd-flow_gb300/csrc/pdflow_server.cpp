@@ -226,6 +226,31 @@ int add_lane(pdflow_server* srv, unsigned width, unsigned height, Lane** out)
         return pdflow::set_error_code(PDFLOW_ERR_OOM, "pinned staging", e);
     }
     L->slot_stream.assign(S, -1);
+    // Warm-up: capture the lane's solve graphs for every batch size now, on
+    // blank frames, so no live request pays for a graph capture.
+    {
+        std::memset(L->st_i, 0, img * S);
+        std::memset(L->st_z, 0, img * S * 2);
+        std::vector<unsigned> slots(S);
+        for (unsigned k = 0; k < S; ++k) slots[k] = k;
+        rc = pdflow_push_frames_slots_u16(L->solver, S, slots.data(), L->st_i, L->st_z);
+        if (!rc) rc = pdflow_push_frames_slots_u16(L->solver, S, slots.data(), L->st_i, L->st_z);
+        for (unsigned n = 1; n <= S && !rc; ++n) {
+            if (srv->cfg.learned) {
+                pdflow_learned_opts o{srv->cfg.iter_scale, srv->cfg.energy_margin};
+                rc = pdflow_solve_slots_learned(L->solver, n, slots.data(), L->net, &o, nullptr);
+            } else {
+                rc = pdflow_solve_slots(L->solver, n, slots.data());
+            }
+            // the plain slot solve is also the fallback path of the learned one
+            if (!rc && srv->cfg.learned) rc = pdflow_solve_slots(L->solver, n, slots.data());
+        }
+        if (!rc) rc = pdflow_synchronize(L->solver);
+        if (rc) {
+            destroy_lane(L.get());
+            return rc;
+        }
+    }
     srv->device_bytes += L->device_bytes;
     Lane* raw = L.get();
     srv->lanes.push_back(std::move(L));

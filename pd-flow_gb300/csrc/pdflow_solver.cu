@@ -195,7 +195,9 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         tiles = forced >= 2 && iters > 0;
         one_launch = forced == 1 && iters > 0 && one_launch_ok;
     } else {
-        tiles = s->iter_form >= 2 && iters > 0 && pl.mode == kIterGrid && pairs > 1;
+        // batches: tiles at every level (measured faster than the cluster-persistent form
+        // from 15x20 up to 120x160 too); a single pair keeps its persistent launch
+        tiles = s->iter_form >= 2 && iters > 0 && pairs > 1;
         one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
     }
     const bool paired = tiles && form >= 3, narrow = form == 4;

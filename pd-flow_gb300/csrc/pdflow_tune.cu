@@ -54,7 +54,7 @@ int pdflow_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_t
         set_last_error("autotuning needs two frames pushed for the whole batch");
         return PDFLOW_ERR_STATE;
     }
-    if (probe_iters == 0) probe_iters = 8;
+    if (probe_iters == 0) probe_iters = 12;   // a multiple of 2, 3 and 4 iterations per launch
     drop_graphs(s);
     const int saved_graph = s->use_graph;
     s->use_graph = 0;

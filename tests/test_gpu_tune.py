@@ -27,7 +27,7 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     lib = _lib.load()
     lib.pdflow_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(Report)]
     rep = Report()
-    assert lib.pdflow_autotune(b.handle, 3, 4, ctypes.byref(rep)) == 0
+    assert lib.pdflow_autotune(b.handle, 3, 12, ctypes.byref(rep)) == 0
     assert rep.levels == 5
     for i in range(rep.levels):
         assert rep.level[i].form in (0, 1, 2, 3, 4)
