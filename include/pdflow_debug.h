@@ -25,10 +25,11 @@ typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const flo
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
 /* Selects how pdflow_solve runs a level's iterations: 4 (default) = every
- * level of a batch (more than one pair) as temporally blocked shared-memory
- * tiles (several iterations per launch; 40x34 tiles, one pixel pair per
- * thread in packed FP32x2 arithmetic), a single pair's levels as one launch
- * per level; 3 = the
+ * level of a batch (more than one pair), and a single pair's levels above
+ * 19 200 pixels, as temporally blocked shared-memory tiles (several
+ * iterations per launch; 40x34 tiles, one pixel pair per thread in packed
+ * FP32x2 arithmetic), a single pair's smaller levels as one launch per
+ * level; 3 = the
  * same with 40x40 tiles and two pairs per thread; 2 = one pixel per lane;
  * 1 = one
  * launch per level (slab-persistent kernel; batches use two kernels per

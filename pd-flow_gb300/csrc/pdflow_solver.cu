@@ -196,8 +196,10 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         one_launch = forced == 1 && iters > 0 && one_launch_ok;
     } else {
         // batches: tiles at every level (measured faster than the cluster-persistent form
-        // from 15x20 up to 120x160 too); a single pair keeps its persistent launch
-        tiles = s->iter_form >= 2 && iters > 0 && pairs > 1;
+        // from 15x20 up to 120x160 too); a single pair: tiles for the levels that would
+        // need the whole grid (240x320, 480x640: 11 % faster per VGA solve), the
+        // one-CTA / cluster persistent launch below
+        tiles = s->iter_form >= 2 && iters > 0 && (pairs > 1 || pl.mode == kIterGrid);
         one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
     }
     const bool paired = tiles && form >= 3, narrow = form == 4;
