@@ -13,10 +13,10 @@
 // beyond the pair needs a scalar load.  Work that depends on a lane's branch
 // (clamping, disc projection with rhypotf, the shrinkage cases) stays scalar.
 //
-// Every valid pixel of the region is updated in every iteration: pixels in the
-// stale ring at a non-border region edge compute garbage from stale
-// neighbours, exactly as they would hold stale values if skipped, and no exact
-// pixel ever reads them.  Reads beyond a region edge are redirected into the
+// A pixel pair is updated in iteration j while at least one of its pixels is
+// j or more from a non-border region edge; the other pixel of such a pair and
+// pixels further out compute garbage from stale neighbours, exactly as they
+// would hold stale values if skipped, and no exact pixel ever reads them.  Reads beyond a region edge are redirected into the
 // region's own storage, so every shared access stays in bounds.
 #include "pdflow_iterate.cuh"
 #include "pdflow_math.cuh"
@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2
 
     const float li = a.p.lambda_i, ld = a.p.lambda_d;
     unsigned flags[kCols];
+    int ring[kCols];       // the pair's larger distance to a non-border region edge
     float2 sg[kCols][8];   // spd*mu, spuvx*li, spuvy*li, spwx*ld, spwy*ld, tau_u, tau_v, tau_w
 #pragma unroll
     for (int c = 0; c < kCols; ++c) {
@@ -228,6 +229,17 @@ __global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2
         if (v0 == R - 1) f |= F_LV0;
         if (v0 + 1 == R - 1) f |= F_LV1;
         flags[c] = f;
+        {
+            // after j iterations only pixels at least j from a non-border region edge
+            // are exact; a pair whose both pixels are closer is skipped from then on
+            int du_ = 1 << 20;
+            if (ru0 > 0) du_ = min(du_, ru);
+            if (ru1 < C) du_ = min(du_, RU - 1 - ru);
+            int d0 = du_, d1 = du_;
+            if (rv0 > 0) { d0 = min(d0, rv); d1 = min(d1, rv + 1); }
+            if (rv1 < R) { d0 = min(d0, RV - 1 - rv); d1 = min(d1, RV - 2 - rv); }
+            ring[c] = (f & F_V1) ? max(d0, d1) : d0;
+        }
         const int q = rv + ru * kRV;
         float s[2][8];
 #pragma unroll
@@ -270,7 +282,7 @@ __global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2
 #pragma unroll
         for (int c = 0; c < kCols; ++c) {
             const unsigned f = flags[c];
-            if (!(f & F_V0)) continue;
+            if (!(f & F_V0) || ring[c] < (int)j) continue;
             const int ru = ty + kTY * c, q = rv + ru * kRV;
             const int qu = (ru + 1 < kRU) ? q + kRV : q;           // beyond the region: own storage
             const int qv = (rv + 2 < kRV) ? q + 2 : q + 1;
@@ -319,7 +331,7 @@ __global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2
 #pragma unroll
         for (int c = 0; c < kCols; ++c) {
             const unsigned f = flags[c];
-            if (!(f & F_V0)) continue;
+            if (!(f & F_V0) || ring[c] < (int)j) continue;
             const int ru = ty + kTY * c, q = rv + ru * kRV;
             const int qm = ru > 0 ? q - kRV : q;                   // beyond the region: own storage
             const int qvm = rv > 0 ? q - 1 : q;
