@@ -400,37 +400,51 @@ __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* dep
 // ---------------------------------------------------------------------------
 // filterSolution (pdflow_cudalib.cu:1040-1148) + computeMotionField (:1150-1167)
 // ---------------------------------------------------------------------------
-// Weighted median of up to 9 samples, register resident.  The reference
-// bubble-sorts (value, weight) pairs (stable: bubbleSortDev swaps only on
-// a[i-1] > a[i]), accumulates the weights in sorted order and walks to the
-// first cumulative weight >= med (pdflow_cudalib.cu:1083-1132).  Here the
-// stable rank of each sample, #{j : f_j < f_i or (f_j == f_i and j < i)},
-// places it directly; every loop is unrolled over constant indices so nothing
-// spills to local memory.  Sums are taken in the same sorted order, so the
-// result and the selected index are the reference's bit for bit.
+// Weighted median of up to 9 samples, register resident (the reference
+// accumulates the weights in sorted order and walks to the first cumulative
+// weight >= med, pdflow_cudalib.cu:1083-1132).
+//
+// Stable sort of up to 9 samples (the reference's bubbleSortDev,
+// pdflow_cudalib.cu:1457-1473, swaps only on a strict '>', so equal values
+// keep their input order) as a 28-comparator sorting network on (value, input
+// index) keys: Batcher's odd-even merge network for 16 inputs restricted to 9,
+// which sorts every 0/1 input and hence every input.  Missing samples (n < 9)
+// enter as (+inf, index >= n) and sort last.  Then the cumulative weights are
+// summed in sorted order, as the reference does, and the bracketing samples
+// are interpolated; the result and the selected index are the reference's bit
+// for bit.  Every index is a compile-time constant: nothing spills.
+__device__ __forceinline__ void cmp_swap(float& fa, float& wa, int& ia, float& fb, float& wb, int& ib)
+{
+    const bool s = (fb < fa) || (fb == fa && ib < ia);
+    const float tf = fa, tw = wa;
+    const int ti = ia;
+    fa = s ? fb : fa;
+    wa = s ? wb : wa;
+    ia = s ? ib : ia;
+    fb = s ? tf : fb;
+    wb = s ? tw : wb;
+    ib = s ? ti : ib;
+}
+
 __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned n, float med_or_neg,
                                          float* total, int32_t* cont_out)
 {
-    int rank[9];
+    float sf[9], sw[9];
+    int id[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
-        int r = 0;
-#pragma unroll
-        for (int j = 0; j < 9; ++j)
-            if (j != i && (unsigned)j < n && (f[j] < f[i] || (f[j] == f[i] && j < i))) ++r;
-        rank[i] = r;
+        const bool in = (unsigned)i < n;
+        sf[i] = in ? f[i] : INFINITY;
+        sw[i] = in ? w[i] : 0.f;
+        id[i] = i;
     }
-    float sf[9], sw[9];
+    constexpr int kNet[28][2] = {{0, 1}, {2, 3}, {0, 2}, {1, 3}, {1, 2}, {4, 5}, {6, 7}, {4, 6}, {5, 7}, {5, 6},
+                                 {0, 4}, {2, 6}, {2, 4}, {1, 5}, {3, 7}, {3, 5}, {1, 2}, {3, 4}, {5, 6}, {0, 8},
+                                 {4, 8}, {2, 4}, {6, 8}, {3, 5}, {1, 2}, {3, 4}, {5, 6}, {7, 8}};
 #pragma unroll
-    for (int r = 0; r < 9; ++r) {
-        sf[r] = 0.f;
-        sw[r] = 0.f;
-#pragma unroll
-        for (int i = 0; i < 9; ++i)
-            if ((unsigned)i < n && rank[i] == r) {
-                sf[r] = f[i];
-                sw[r] = w[i];
-            }
+    for (int c = 0; c < 28; ++c) {
+        const int a = kNet[c][0], b = kNet[c][1];
+        cmp_swap(sf[a], sw[a], id[a], sf[b], sw[b], id[b]);
     }
     float cum[9];
     cum[0] = sw[0];

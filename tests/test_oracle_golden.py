@@ -8,6 +8,8 @@ FP32 rounding in every set-up stage and, after hundreds of non-smooth
 iterations, to ~1e-6 m in the mean with a handful of near-tie pixels (median /
 L1-shrinkage branch flips) further out.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -116,3 +118,32 @@ def test_oracle_level_state_tracks_reference(golden_qvga, oracle_r60_dumps, fiel
     ours = oracle_r60_dumps[(field, level)]
     d = np.abs(ours.astype(np.float64) - ref)
     assert d.mean() <= 1e-4 * max(1.0, np.abs(ref).mean() * 100), (field, level, d.mean())
+
+
+def test_median_sorting_network_sorts_every_zero_one_input():
+    """The 9-input comparator network of k_median (Batcher's odd-even merge
+    network for 16 inputs restricted to 9) sorts all 512 zero-one inputs, so
+    by the 0-1 principle it sorts every input; with (value, input index) keys
+    it reproduces the stable order of the reference's bubble sort."""
+    import itertools
+    import re
+    src = open(os.path.join(os.path.dirname(__file__), "..", "pd-flow_gb300", "csrc", "pdflow_kernels.cu")).read()
+    body = src[src.index("kNet[28][2] = {"):]
+    body = body[:body.index("};")]
+    net = [tuple(map(int, m)) for m in re.findall(r"\{(\d+), (\d+)\}", body)]
+    assert len(net) == 28
+    for bits in itertools.product((0, 1), repeat=9):
+        x = list(bits)
+        for a, b in net:
+            if x[b] < x[a]:
+                x[a], x[b] = x[b], x[a]
+        assert x == sorted(x)
+    # stable order on ties with (value, index) keys
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        vals = rng.integers(0, 3, size=9).astype(float)
+        keys = [(v, i) for i, v in enumerate(vals)]
+        for a, b in net:
+            if keys[b] < keys[a]:
+                keys[a], keys[b] = keys[b], keys[a]
+        assert [i for _, i in keys] == sorted(range(9), key=lambda i: (vals[i], i))
