@@ -42,7 +42,8 @@ extern "C" {
 int pdflow_read_level_images(pdflow_solver* s, unsigned level, int frame, float* colour, float* depth, float* xx,
                              float* yy)
 {
-    if (!s || level >= s->pyr_levels || (frame != 0 && frame != 1)) return PDFLOW_ERR_ARG;
+    if (!s || level >= s->pyr_levels || (frame != 0 && frame != 1))
+        return fail(PDFLOW_ERR_ARG, "level beyond the pyramid or frame not 0/1");
     const PyrLevel& P = s->pyr[frame ? s->new_slot : (s->new_slot ^ 1)][level];
     const size_t n = (size_t(s->width) >> level) * (size_t(s->height) >> level);
     const float* src[4] = {P.col, P.dep, P.xx, P.yy};
@@ -79,8 +80,8 @@ int pdflow_read_all_solutions(pdflow_solver* s, float* dx, float* dy, float* dz,
 
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 {
-    if (!s || !fn) return PDFLOW_ERR_ARG;
-    if (s->frames < 2) return PDFLOW_ERR_STATE;
+    if (!s || !fn) return fail(PDFLOW_ERR_ARG, "null argument");
+    if (s->frames < 2) return fail(PDFLOW_ERR_STATE, "solve needs two pushed frames");
     cudaStream_t st = s->stream;
     Dumper dump{fn, ctx, st, {}};
     Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
@@ -143,19 +144,22 @@ int pdflow_set_iteration_form(pdflow_solver* s, int form)
 
 int pdflow_last_solve_launches(const pdflow_solver* s, unsigned* count)
 {
-    if (!s || !count) return PDFLOW_ERR_ARG;
+    if (!s || !count) return fail(PDFLOW_ERR_ARG, "null argument");
     *count = s->launches;
     return PDFLOW_OK;
 }
 
 int pdflow_time_level_iterations(pdflow_solver* s, unsigned n, unsigned level, unsigned iters, float* ms)
 {
-    if (!s || !ms || n == 0 || n > s->batch || level >= s->ctf_levels || iters == 0) return PDFLOW_ERR_ARG;
+    if (!s || !ms || n == 0 || n > s->batch || level >= s->ctf_levels || iters == 0)
+        return fail(PDFLOW_ERR_ARG, "bad pair count, level or iteration count");
     cudaEvent_t a, b;
-    if (cudaEventCreate(&a) != cudaSuccess) return PDFLOW_ERR_CUDA;
-    if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaError_t ce = cudaEventCreate(&a);
+    if (ce != cudaSuccess) return fail("event create", ce);
+    ce = cudaEventCreate(&b);
+    if (ce != cudaSuccess) {
         cudaEventDestroy(a);
-        return PDFLOW_ERR_CUDA;
+        return fail("event create", ce);
     }
     cudaEventRecord(a, s->stream);
     int rc = enqueue_level_iterations(s, s->stream, n, level, iters);
@@ -172,7 +176,8 @@ int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const fl
                         const float* dv, const float* dw, float* du_l, float* dv_l, float* dw_l, int32_t* sel,
                         void* stream)
 {
-    if (!depth_old || !ddt || !du || !dv || !dw || !du_l || !dv_l || !dw_l || R < 2 || C < 2) return PDFLOW_ERR_ARG;
+    if (!depth_old || !ddt || !du || !dv || !dw || !du_l || !dv_l || !dw_l || R < 2 || C < 2)
+        return fail(PDFLOW_ERR_ARG, "null plane or level smaller than 2x2");
     LevelGeom g{R, C, R * C};  // one pair, no stride
     PyrLevel o{nullptr, const_cast<float*>(depth_old), nullptr, nullptr};
     LevelConsts L{};
