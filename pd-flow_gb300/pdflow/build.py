@@ -5,7 +5,8 @@
 Each translation unit under csrc/ is compiled in parallel by nvcc with
 `-gencode arch=compute_103a,code=sm_103a -lineinfo -O3`; the objects are
 linked into lib/libpdflow_gb300.so (a C ABI: include/pdflow.h).  The ptxas
-resource report of every kernel is kept in lib/ptxas.log.
+resource report of every kernel (of all translation units, also those not
+recompiled) is kept in lib/ptxas.log.
 """
 from __future__ import annotations
 
@@ -55,13 +56,16 @@ def _stale(target: str, deps) -> bool:
 def _compile(src: str):
     obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
     if not _stale(obj, [src] + _headers()):
-        return obj, ""
+        rep = obj + ".ptxas"
+        return obj, open(rep).read() if os.path.exists(rep) else ""
     cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
            "-Xptxas", "-v", "--expt-relaxed-constexpr", "-I", os.path.join(REPO_ROOT, "include"),
            "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+    with open(obj + ".ptxas", "w") as f:
+        f.write(r.stderr)
     return obj, r.stderr
 
 
@@ -72,10 +76,9 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         results = list(ex.map(_compile, srcs))
     objs = [o for o, _ in results]
-    logs = "".join(l for _, l in results)
-    if logs:
-        with open(os.path.join(LIBDIR, "ptxas.log"), "w") as f:
-            f.write(logs)
+    logs = "".join(l for _, l in results)     # every translation unit's report, fresh or kept
+    with open(os.path.join(LIBDIR, "ptxas.log"), "w") as f:
+        f.write(logs)
     if _stale(LIB_PATH, objs):
         cuda_lib = os.path.join(_cuda_home(), "lib64")
         cmd = [_nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB_PATH, *objs,
