@@ -179,6 +179,25 @@ int pdflow_solve_slots(pdflow_solver* s, unsigned n, const unsigned* slots);
 /* Copies the listed slots' motion fields to host arrays [n][rows*cols]. */
 int pdflow_read_flow_slots(pdflow_solver* s, unsigned n, const unsigned* slots, float* dx, float* dy, float* dz);
 
+/* ---- Mixed-resolution batches (no counterpart in the reference) ----
+ * One handle holds pairs of different rows (15..480; rows 480 take 640x480
+ * frames, smaller rows 320x240 frames, as the reference's cam_mode) and
+ * solves them with one launch per kernel per coarse-to-fine step: all rows
+ * classes share the 15x20 -> 480x640 ladder, so at every step the pairs that
+ * have that level solve the same size.  Each pair's iteration schedule is the
+ * reference default for its rows, and each pair's result equals a single-pair
+ * solve of the same frames, bit for bit.  Iterations run in the tile form. */
+int pdflow_create_mixed(unsigned max_pairs, pdflow_solver** out);
+/* Pushes one frame for each of pairs [0, n): rows[k] is pair k's rows; the
+ * frames of the rows-480 pairs come, in pair order, from vga_* ([m][480][640])
+ * and the others' from qvga_* ([m'][240][320]).  A rows vector that differs
+ * from the previous push starts new pairs. */
+int pdflow_push_frames_mixed(pdflow_solver* s, unsigned n, const unsigned* rows, const uint8_t* vga_intensity,
+                             const uint16_t* vga_depth, const uint8_t* qvga_intensity, const uint16_t* qvga_depth);
+int pdflow_solve_mixed(pdflow_solver* s, unsigned n);
+/* Copies pair k's motion field (rows_k x cols_k floats each) to host memory; blocks. */
+int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, float* dz);
+
 /* ---- Launch-form autotuner (no counterpart in the reference) ----
  * A level's iterations can run as two kernels per iteration (form 0), one
  * persistent launch per level (form 1: one CTA, a cluster, or, for a single

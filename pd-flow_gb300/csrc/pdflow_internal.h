@@ -58,6 +58,14 @@ struct pdflow_solver {
         unsigned launches;
     };
     std::vector<GraphEntry> graphs;      // captured solves, per (slot, pair count, iteration form)
+    // mixed-resolution batches (pdflow_mixed.cu): VGA-sized slots holding pairs of any rows
+    int mixed = 0;
+    std::vector<unsigned> mixed_rows;    // rows of the pair in each slot (0: none)
+    unsigned* map_table = nullptr;       // device: the slot maps of every launch of the mixed plan
+    size_t map_table_cap = 0;
+    std::vector<unsigned> plan_rows;     // rows vector the current table / graph were built for
+    cudaGraphExec_t mixed_graph = nullptr;
+    int mixed_graph_slot = -1;
 };
 
 namespace pdflow {

@@ -470,13 +470,15 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
     return median_lerp(cr, cl, med, fl, fr);
 }
 
-__global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, LevelSol out, float* dx,
-                         float* dy, float* dz, Params p, int32_t* sel)
+__global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, State Salt, LevelSol out,
+                         float* dx, float* dy, float* dz, Params p, int32_t* sel)
 {
     const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
+    const unsigned pf = pair_flags(g.map, blockIdx.y);
+    finest = finest || (pf & kMapFinest);
     o = at(o, po);
     L = at(L, po);
-    S = at(S, po);
+    S = at((pf & kMapAlt) ? Salt : S, po);
     out = at(out, po);
     dx = at(dx, po);
     dy = at(dy, po);
@@ -536,7 +538,8 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     out.pwv[index] = S.pwv[index];
     if (finest) {
         if (depth_old > 0) {
-            motion_field(depth_old, ru, rv, rw, o.xx[index], o.yy[index], inv_focal(p.fovh, p.cols), dx[index],
+            // the finest level is cols wide (g.C == p.cols), also for a mixed batch's smaller pairs
+            motion_field(depth_old, ru, rv, rw, o.xx[index], o.yy[index], inv_focal(p.fovh, g.C), dx[index],
                          dy[index], dz[index]);
         } else {
             dx[index] = 0.f;
@@ -688,9 +691,9 @@ cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* de
 }
 
 cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out, float* dx,
-                          float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st)
+                          float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st, const State* alt)
 {
-    k_median<<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, out, dx, dy, dz, p, sel);
+    k_median<<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p, sel);
     return cudaGetLastError();
 }
 

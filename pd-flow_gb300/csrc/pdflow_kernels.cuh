@@ -44,11 +44,22 @@ struct LevelGeom {
     const unsigned* map = nullptr;   // device [pairs]: arena slot of grid index y (null: slot y)
 };
 
+// A map entry is an arena slot in its low 28 bits plus per-pair flags used by
+// mixed-resolution batches, whose pairs end their levels at different steps.
+constexpr unsigned kMapSlotMask = 0x0FFFFFFFu;
+constexpr unsigned kMapLast = 1u << 31;     // tile launch: it ends the pair's level (saturate)
+constexpr unsigned kMapFinest = 1u << 30;   // median: the pair's finest level (motion field)
+constexpr unsigned kMapAlt = 1u << 29;      // median: the pair's final state is in the second buffers
+
 #ifdef __CUDACC__
 // Byte offset of the arena slot that grid index y works on.
 __device__ __forceinline__ size_t pair_off(const unsigned* map, size_t pstride, unsigned y)
 {
-    return (size_t)(map ? __ldg(map + y) : y) * pstride;
+    return (size_t)(map ? (__ldg(map + y) & kMapSlotMask) : y) * pstride;
+}
+__device__ __forceinline__ unsigned pair_flags(const unsigned* map, unsigned y)
+{
+    return map ? (__ldg(map + y) & ~kMapSlotMask) : 0u;
 }
 #endif
 
@@ -121,7 +132,10 @@ cudaError_t launch_dual(LevelGeom g, LevelConsts L, State S, Params p, cudaStrea
 cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old,
                           cudaStream_t st);
 cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old, cudaStream_t st);
+// `alt`: the second state buffers, read instead of S by pairs whose map entry
+// carries kMapAlt (mixed batches); kMapFinest marks a pair's finest level.
 cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out,
-                          float* dx, float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st);
+                          float* dx, float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st,
+                          const State* alt = nullptr);
 
 }  // namespace pdflow

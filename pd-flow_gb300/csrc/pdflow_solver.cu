@@ -503,6 +503,8 @@ int pdflow_destroy(pdflow_solver* s)
     cudaStreamSynchronize(s->stream);
     for (auto& g : s->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (s->mixed_graph) cudaGraphExecDestroy(s->mixed_graph);
+    if (s->map_table) cudaFree(s->map_table);
     cudaFree(s->arena);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;

@@ -276,8 +276,9 @@ __global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2
     const float2 li2 = make_float2(li, li), ld2v = make_float2(ld, ld), two = make_float2(2.f, 2.f);
     const float2 zero = make_float2(0.f, 0.f);
 
+    const bool last_launch = a.last || (pair_flags(a.g.map, blockIdx.y) & kMapLast);
     for (unsigned j = 0; j < a.kk; ++j) {
-        const bool last_iter = a.last && (j + 1 == a.kk);
+        const bool last_iter = last_launch && (j + 1 == a.kk);
         // ---- dual step (in place: each pixel reads only its own duals) ----
 #pragma unroll
         for (int c = 0; c < kCols; ++c) {

@@ -160,6 +160,10 @@ _SIGNATURES = {
     "pdflow_set_level_form": (ctypes.c_int, [vp, u32, ctypes.c_int, u32]),
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),
+    "pdflow_push_frames_mixed": (ctypes.c_int, [vp, u32, vp, vp, vp, vp, vp]),
+    "pdflow_solve_mixed": (ctypes.c_int, [vp, u32]),
+    "pdflow_read_flow_mixed": (ctypes.c_int, [vp, u32, vp, vp, vp]),
     "pdflow_gemm_bf16": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int,
                                         vp, ctypes.c_int, ctypes.c_int, vp]),
 }
@@ -502,6 +506,58 @@ class BatchSolver(_Extras):
         a, b = np.zeros(n, np.float32), np.zeros(n, np.float32)
         check(load().pdflow_learned_energies(self._h, n, _ptr(a), _ptr(b)), "pdflow_learned_energies")
         return a, b
+
+    def close(self):
+        if self._h is not None:
+            load().pdflow_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MixedBatch:
+    """Pairs of different rows (15..480) solved together (pdflow_create_mixed):
+    push(rows, frames) with frames[k] = (intensity, depth) of pair k (640x480
+    for rows 480, 320x240 otherwise), then solve() and flow(k)."""
+
+    def __init__(self, max_pairs: int, use_graph: bool = True):
+        h = ctypes.c_void_p()
+        check(load().pdflow_create_mixed(max_pairs, ctypes.byref(h)), "pdflow_create_mixed")
+        self._h = h
+        self.rows = []
+        check(load().pdflow_set_graph_mode(h, int(use_graph)), "pdflow_set_graph_mode")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def push(self, rows, intensity, depth):
+        rows = [int(r) for r in rows]
+        sel = lambda big: [k for k, r in enumerate(rows) if (r == 480) == big]
+        stack = lambda ks, a, dt: (np.ascontiguousarray(np.stack([a[k] for k in ks]), dt) if ks else None)
+        vi, vz = stack(sel(True), intensity, np.uint8), stack(sel(True), depth, np.uint16)
+        qi, qz = stack(sel(False), intensity, np.uint8), stack(sel(False), depth, np.uint16)
+        r = np.ascontiguousarray(rows, np.uint32)
+        p = lambda a: _ptr(a) if a is not None else None
+        check(load().pdflow_push_frames_mixed(self._h, len(rows), _ptr(r), p(vi), p(vz), p(qi), p(qz)),
+              "pdflow_push_frames_mixed")
+        self.rows = rows
+
+    def solve(self, n: int | None = None):
+        check(load().pdflow_solve_mixed(self._h, n or len(self.rows)), "pdflow_solve_mixed")
+
+    def flow(self, k: int):
+        r = self.rows[k]
+        out = [np.zeros(r * (r * 4 // 3), np.float32) for _ in range(3)]
+        check(load().pdflow_read_flow_mixed(self._h, k, *[_ptr(a) for a in out]), "pdflow_read_flow_mixed")
+        return out
+
+    def synchronize(self):
+        check(load().pdflow_synchronize(self._h), "pdflow_synchronize")
 
     def close(self):
         if self._h is not None:
