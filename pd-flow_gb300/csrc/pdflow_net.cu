@@ -25,6 +25,7 @@
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -406,6 +407,21 @@ struct pdflow_net {
 namespace {
 
 thread_local std::string g_net_error;
+
+// The GEMM kernel's shared-memory attribute, once per device, under a lock.
+cudaError_t prepare_gemm_once()
+{
+    static std::mutex mu;
+    static unsigned long long prepared = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 64 && ((prepared >> dev) & 1ull)) return cudaSuccess;
+    e = prepare_gemm_tc();
+    if (e == cudaSuccess && dev < 64) prepared |= 1ull << dev;
+    return e;
+}
 
 int net_fail(int code, const char* what, cudaError_t e = cudaSuccess)
 {
@@ -802,13 +818,7 @@ int pdflow_net_create(unsigned max_batch, unsigned long long seed, pdflow_net** 
     NET_TRY(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
     if (!(prop.major == 10 && prop.minor == 3))
         return net_fail(PDFLOW_ERR_NO_DEVICE, "this library is built for sm_103a (GB300) only");
-    {
-        static bool prepared = false;
-        if (!prepared) {
-            NET_TRY(prepare_gemm_tc(), "GEMM kernel attributes");
-            prepared = true;
-        }
-    }
+    NET_TRY(prepare_gemm_once(), "GEMM kernel attributes");
     pdflow_net* n = new (std::nothrow) pdflow_net();
     if (!n) return net_fail(PDFLOW_ERR_OOM, "host allocation");
     n->max_batch = max_batch;
@@ -979,13 +989,7 @@ int pdflow_gemm_bf16(int M, int N, int K, const void* d_a, int lda, const void* 
                      int k_per_split, void* stream)
 {
     if (!d_a || !d_b || !d_c) return net_fail(PDFLOW_ERR_ARG, "null argument");
-    {
-        static bool prepared = false;
-        if (!prepared) {
-            NET_TRY(prepare_gemm_tc(), "GEMM kernel attributes");
-            prepared = true;
-        }
-    }
+    NET_TRY(prepare_gemm_once(), "GEMM kernel attributes");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const unsigned splits = k_per_split > 0 ? gemm_splits(K, k_per_split) : 1u;
     float* part = nullptr;

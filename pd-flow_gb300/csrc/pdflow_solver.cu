@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -444,12 +445,15 @@ int pdflow_create_batch(unsigned rows, unsigned width, unsigned height, const pd
     if (!(prop.major == 10 && prop.minor == 3))
         return set_error(PDFLOW_ERR_NO_DEVICE, "this library is built for sm_103a (GB300) only");
     {
-        static bool prepared = false;
-        if (!prepared) {
+        // kernel attributes are per device: set them once per device, under a lock
+        static std::mutex mu;
+        static unsigned long long prepared = 0;
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev >= 64 || !((prepared >> dev) & 1ull)) {
             CUDA_TRY(prepare_iterate(), "kernel attributes");
             CUDA_TRY(prepare_tiles(), "kernel attributes");
             CUDA_TRY(prepare_tiles2(), "kernel attributes");
-            prepared = true;
+            if (dev < 64) prepared |= 1ull << dev;
         }
     }
 
