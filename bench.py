@@ -302,7 +302,8 @@ def ours(args):
     with torch.cuda.stream(stream):
         push()
         b.synchronize()
-        tune = autotune(lib, b.handle, B)
+        tune = [{k: (v if k != "ms_per_iter" else [None if x is None else round(x, 4) for x in v])
+                 for k, v in lvl.items()} for lvl in b.autotune(B)]
         push()
         b.solve(B)
         plain_b = b.read_flow(B)
@@ -532,24 +533,6 @@ def mixed_batch_run(torch, steps=5, n=64, seed0=5_000_000):
     counts = {r: rows.count(r) for r in (60, 120, 240, 480)}
     return {"pairs_s": n / (ms / 1000.0), "ms_per_batch": ms, "pairs": n, "rows_counts": counts,
             "workload": "plain schedule, rows uniform in {60,120,240,480}, one launch per kernel per level size"}
-
-
-def autotune(lib, handle, n):
-    """Per-level launch forms for this batch (pdflow_autotune)."""
-
-    class Level(ctypes.Structure):
-        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 11)]
-
-    class Report(ctypes.Structure):
-        _fields_ = [("levels", ctypes.c_uint), ("level", Level * 8)]
-
-    rep = Report()
-    lib.pdflow_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(Report)]
-    from pdflow import _lib
-    _lib.check(lib.pdflow_autotune(handle, n, 12, ctypes.byref(rep)), "pdflow_autotune")
-    return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
-             "ms_per_iter": [None if not np.isfinite(x) else round(float(x), 4) for x in rep.level[i].ms_per_iter]}
-            for i in range(rep.levels)]
 
 
 def reference_cuda_timing():

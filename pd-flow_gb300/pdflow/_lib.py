@@ -32,6 +32,20 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
+TUNE_CANDIDATES = 11   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2/3/4 x {2, 3, 4} iterations per launch
+
+
+class TuneLevel(ctypes.Structure):
+    """pdflow_tune_level (include/pdflow.h)."""
+    _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint),
+                ("ms_per_iter", ctypes.c_float * TUNE_CANDIDATES)]
+
+
+class TuneReport(ctypes.Structure):
+    """pdflow_tune_report (include/pdflow.h)."""
+    _fields_ = [("levels", ctypes.c_uint), ("level", TuneLevel * 8)]
+
+
 class LearnedOpts(ctypes.Structure):
     """pdflow_learned_opts (include/pdflow_net.h)."""
     _fields_ = [("iter_scale", ctypes.c_float), ("energy_margin", ctypes.c_float)]
@@ -158,6 +172,7 @@ _SIGNATURES = {
     "pdflow_seed_level_inputs": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_seed_level_labels": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_set_level_form": (ctypes.c_int, [vp, u32, ctypes.c_int, u32]),
+    "pdflow_autotune": (ctypes.c_int, [vp, u32, u32, ctypes.POINTER(TuneReport)]),
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),
@@ -481,6 +496,18 @@ class BatchSolver(_Extras):
         check(load().pdflow_read_flow_slots(self._h, len(sl), _ptr(sl), *[_ptr(a) for a in out]),
               "pdflow_read_flow_slots")
         return out
+
+    def autotune(self, n: int, probe_iters: int = 12):
+        """Per-level launch form and iterations per launch for pairs [0, n)
+        (pdflow_autotune); returns [{form, iters_per_launch, ms_per_iter}] per level."""
+        rep = TuneReport()
+        check(load().pdflow_autotune(self._h, n, probe_iters, ctypes.byref(rep)), "pdflow_autotune")
+        return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
+                 "ms_per_iter": [None if not np.isfinite(x) else float(x) for x in rep.level[i].ms_per_iter]}
+                for i in range(rep.levels)]
+
+    def set_level_form(self, level: int, form: int, iters_per_launch: int = 0):
+        check(load().pdflow_set_level_form(self._h, level, form, iters_per_launch), "pdflow_set_level_form")
 
     def solve_learned(self, n: int, net: "Net", iter_scale: float = 0.5, energy_margin: float = 0.01):
         """Learned warm-start solve of pairs [0, n) (pdflow_solve_batch_learned)."""

@@ -18,26 +18,17 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     b.solve(3)
     ref = b.read_flow(3)
 
-    class Level(ctypes.Structure):
-        _fields_ = [("form", ctypes.c_int), ("iters_per_launch", ctypes.c_uint), ("ms_per_iter", ctypes.c_float * 11)]
-
-    class Report(ctypes.Structure):
-        _fields_ = [("levels", ctypes.c_uint), ("level", Level * 8)]
-
     lib = _lib.load()
-    lib.pdflow_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(Report)]
-    rep = Report()
-    assert lib.pdflow_autotune(b.handle, 3, 12, ctypes.byref(rep)) == 0
-    assert rep.levels == 5
-    for i in range(rep.levels):
-        assert rep.level[i].form in (0, 1, 2, 3, 4)
-        assert np.isfinite(rep.level[i].ms_per_iter[0])
+    rep = b.autotune(3)
+    assert len(rep) == 5
+    for lvl in rep:
+        assert lvl["form"] in (0, 1, 2, 3, 4)
+        assert lvl["ms_per_iter"][0] is not None
     b.solve(3)
     got = b.read_flow(3)
     for x, y in zip(got, ref):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
     # each tile width of iterations per launch, forced on every level
-    lib.pdflow_set_level_form.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_uint]
     for form, kk in ((2, 1), (2, 2), (2, 3), (3, 1), (3, 2), (3, 3), (3, 4), (4, 1), (4, 3), (4, 4)):
         for lvl in range(5):
             assert lib.pdflow_set_level_form(b.handle, lvl, form, kk) == 0
