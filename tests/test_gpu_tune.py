@@ -39,22 +39,26 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     b.close()
 
 
+DEFAULT_COPY_MODE = {3: 1, 4: 0}   # the library's defaults (pdflow_tiles2.cu)
+
+
 @pytest.mark.parametrize("form", [3, 4])
 def test_tile_copy_modes_give_the_same_bits(built_lib, form):
     import ctypes
     from pdflow import _lib
     lib = _lib.load()
-    pairs = [scenes.make_pair(950 + k) for k in range(2)]
+    n = 4
+    pairs = [scenes.make_pair(950 + k) for k in range(n)]
     out = []
-    for mode in (0, 1, 2, 3):
+    for mode in range(4):
         assert lib.pdflow_set_tile_copy_mode(form - 3, mode) == 0
-        b = BatchSolver(240, 320, 240, 2, iteration_form=form)
+        b = BatchSolver(240, 320, 240, n, iteration_form=form)
         b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
         b.push_raw(np.stack([p[2] for p in pairs]), np.stack([p[3] for p in pairs]))
-        b.solve(2)
-        out.append(b.read_flow(2))
+        b.solve(n)
+        out.append(b.read_flow(n))
         b.close()
-    lib.pdflow_set_tile_copy_mode(form - 3, 1 if form == 3 else 0)
+    lib.pdflow_set_tile_copy_mode(form - 3, DEFAULT_COPY_MODE[form])
     for o in out[1:]:
         for x, y in zip(o, out[0]):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
