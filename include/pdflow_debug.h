@@ -24,17 +24,17 @@ typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const flo
  * in CSF_cuda, pdflow_cudalib.h:71-122).  The final flow equals pdflow_solve's. */
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
-/* Selects how pdflow_solve runs a level's iterations: 4 (default) = every
+/* Selects how pdflow_solve runs a level's iterations: 5 (default) = every
  * level of a batch (more than one pair), and a single pair's levels above
  * 19 200 pixels, as temporally blocked shared-memory tiles (several
- * iterations per launch; 40x34 tiles, one pixel pair per thread in packed
- * FP32x2 arithmetic), a single pair's smaller levels as one launch per
- * level; 3 = the
- * same with 40x40 tiles and two pairs per thread; 2 = one pixel per lane;
- * 1 = one
- * launch per level (slab-persistent kernel; batches use two kernels per
- * iteration for the large levels); 0 = two kernels per iteration (the
- * reference's launch structure with gradient+dual and divergence+primal
+ * iterations per launch; 24x24 tiles, one pixel pair per thread in packed
+ * FP32x2 arithmetic, two CTAs per SM so that one CTA's region load and store
+ * overlap the other's iterations), a single pair's smaller levels as one
+ * launch per level; 4 = the same with 40x34 tiles (1008 threads, one CTA per
+ * SM); 3 = the same with 40x40 tiles and two pairs per thread; 2 = one pixel
+ * per lane; 1 = one launch per level (slab-persistent kernel; batches use two
+ * kernels per iteration for the large levels); 0 = two kernels per iteration
+ * (the reference's launch structure with gradient+dual and divergence+primal
  * fused).  All give the same bits. */
 int pdflow_set_iteration_form(pdflow_solver* s, int form);
 
@@ -70,7 +70,8 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
 
 /* How the paired tile kernels move a tile's region between HBM and shared
  * memory (process-wide; graphs captured afterwards use it): shape 0 = 40x40
- * tiles (iteration form 3), 1 = 40x34 tiles (form 4); mode bit 0 = TMA bulk
+ * tiles (iteration form 3), 1 = 40x34 tiles (form 4), 2 = 24x24 tiles
+ * (form 5); mode bit 0 = TMA bulk
  * copies for the region load, bit 1 = for the interior store, else plain
  * loads/stores.  Levels whose row count is not a multiple of 4 always use
  * plain loads and stores.  All modes give the same bits. */

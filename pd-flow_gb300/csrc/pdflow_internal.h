@@ -24,6 +24,7 @@ struct pdflow_solver {
     float* stage_Z = nullptr;
     uint8_t* stage_u8 = nullptr;         // device staging of a raw frame
     uint16_t* stage_u16 = nullptr;
+    uint8_t* stage_rgb = nullptr;        // device staging of RGB888 frames (allocated on first use)
     pdflow::LevelConsts L{};
     pdflow::State S{};
     float* alt[10] = {};                 // second buffer of du_acc,dv_acc,dw_acc,pd,puu,puv,pvu,pvv,pwu,pwv
@@ -32,7 +33,8 @@ struct pdflow_solver {
     unsigned* flags = nullptr;           // per-CTA progress counters of the grid-form iteration
     unsigned* status = nullptr;          // device status word (0 = ok)
     int num_sms = 0;
-    int iter_form = 4;                   // 4 / 3 / 2 = narrow paired / paired / scalar tiles for large levels,
+    int iter_form = 5;                   // 5 / 4 / 3 = paired tiles 24x24 (two CTAs per SM) / 40x34 / 40x40,
+                                         // 2 = scalar tiles for large levels,
                                          // 1 = one launch per level, 0 = two kernels per iteration
     int level_form[8] = {-1, -1, -1, -1, -1, -1, -1, -1};   // per-level override (autotuner); -1 = iter_form's choice
     unsigned level_kk[8] = {};           // tile form: iterations per launch (0 = the halo width)

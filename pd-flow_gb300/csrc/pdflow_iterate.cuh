@@ -49,11 +49,12 @@ unsigned tiles_per_level(LevelGeom g);
 cudaError_t launch_iterate_tiles(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
                                  unsigned kk, bool last, cudaStream_t st);
 // The paired FP32x2 variant of the same tiling (pdflow_tiles2.cu); same bits.
-// set_tile_copy_mode(shape 0 = 40x40 / 1 = 40x34, bit 0 = bulk load, bit 1 = bulk store).
+// Shapes: 0 = 40x40 tiles (iteration form 3), 1 = 40x34 (form 4), 2 = 24x24
+// (form 5, two CTAs per SM).  set_tile_copy_mode: bit 0 = bulk load, bit 1 = bulk store.
 void set_tile_copy_mode(int shape, int mode);
 cudaError_t prepare_tiles2();
 cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
-                                  unsigned kk, bool last, cudaStream_t st, bool narrow = false,
+                                  unsigned kk, bool last, cudaStream_t st, int shape = 0,
                                   unsigned* status = nullptr);
 // Enqueues the level's iterations (and, in the grid form, the reset of the progress counters).
 cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st);

@@ -102,7 +102,8 @@ int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec
             cur = s->S;
             nxt = alt;
         } else if (r.kind == 1) {
-            e = launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, r.kk, false, st, true, s->status);
+            const int shape = s->iter_form >= 3 ? s->iter_form - 3 : 2;   // the paired tiles of the handle's form
+            e = launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, r.kk, false, st, shape, s->status);
             std::swap(cur, nxt);
             *count += 1;
         } else {

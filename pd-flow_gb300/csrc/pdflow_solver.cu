@@ -203,7 +203,8 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         tiles = s->iter_form >= 2 && iters > 0 && (pairs > 1 || pl.mode == kIterGrid);
         one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
     }
-    const bool paired = tiles && form >= 3, narrow = form == 4;
+    const bool paired = tiles && form >= 3;
+    const int shape = form - 3;   // 40x40, 40x34 or 24x24 tiles
     if (tiles) {
         State cur = s->S;
         State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
@@ -214,7 +215,7 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         for (unsigned done = 0; done < iters;) {
             const unsigned kk = (iters - done < h) ? iters - done : h;
             if (paired)
-                CUDA_TRY(launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, narrow,
+                CUDA_TRY(launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, shape,
                                                s->status),
                          "tile iteration launch");
             else
@@ -509,6 +510,7 @@ int pdflow_destroy(pdflow_solver* s)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (s->mixed_graph) cudaGraphExecDestroy(s->mixed_graph);
     if (s->map_table) cudaFree(s->map_table);
+    if (s->stage_rgb) cudaFree(s->stage_rgb);
     cudaFree(s->arena);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
@@ -566,6 +568,43 @@ int pdflow_push_frames_u16(pdflow_solver* s, unsigned n, const uint8_t* intensit
 int pdflow_push_frame_u16(pdflow_solver* s, const uint8_t* intensity, const uint16_t* depth)
 {
     return pdflow_push_frames_u16(s, 1, intensity, depth);
+}
+
+int pdflow_push_frames_rgb8_mm_device(pdflow_solver* s, unsigned n, const uint8_t* d_rgb, const uint16_t* d_depth_mm,
+                                      int rotate180)
+{
+    if (!s || !d_rgb || !d_depth_mm) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    s->new_slot ^= 1;
+    CUDA_TRY(launch_decode_rgb8_mm(d_rgb, d_depth_mm, s->width, s->height, s->pyr[s->new_slot][0], s->prm.fovh, n,
+                                   s->pair_stride, s->stream, rotate180 ? 1 : 0),
+             "RGB decode launch");
+    return push_common(s, n);
+}
+
+int pdflow_push_frames_rgb8_mm(pdflow_solver* s, unsigned n, const uint8_t* rgb, const uint16_t* depth_mm,
+                               int rotate180)
+{
+    if (!s || !rgb || !depth_mm) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t px = size_t(s->width) * s->height * n;
+    if (!s->stage_rgb) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, size_t(s->width) * s->height * 3 * s->batch) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(PDFLOW_ERR_OOM, "RGB staging buffer");
+        }
+        s->stage_rgb = static_cast<uint8_t*>(p);
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->stage_rgb, rgb, px * 3, cudaMemcpyHostToDevice, s->stream), "H2D RGB");
+    CUDA_TRY(cudaMemcpyAsync(s->stage_u16, depth_mm, px * 2, cudaMemcpyHostToDevice, s->stream), "H2D depth");
+    return pdflow_push_frames_rgb8_mm_device(s, n, s->stage_rgb, s->stage_u16, rotate180);
+}
+
+int pdflow_push_frame_rgb8_mm(pdflow_solver* s, const uint8_t* rgb, const uint16_t* depth_mm, int rotate180)
+{
+    return pdflow_push_frames_rgb8_mm(s, 1, rgb, depth_mm, rotate180);
 }
 
 int pdflow_solve_batch(pdflow_solver* s, unsigned n)

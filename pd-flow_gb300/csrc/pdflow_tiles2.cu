@@ -3,8 +3,9 @@
 // Same tiling as pdflow_tiles.cu (40x40 interior, 4-pixel halo, 48x48 region
 // of 24 planes in shared memory, kk <= 4 iterations per launch, alternating
 // state buffers), but each of the 576 threads owns two vertically adjacent
-// pixel pairs (v, v+1) in each of two region columns (or, in the narrow
-// shape, 40x34 interiors and 1008 threads owning one pair each).  A pair's arithmetic
+// pixel pairs (v, v+1) in each of two region columns (or, in the narrower
+// shapes, 40x34 interiors and 1008 threads, or 24x24 interiors and 512
+// threads, each thread owning one pair).  A pair's arithmetic
 // runs as packed FP32x2 instructions (fma/add/sub/mul.rn.f32x2: each lane
 // rounds exactly as the scalar __f*_rn operation, so the results are the
 // same bits as the scalar kernels, as long as no packed product feeds only a
@@ -25,20 +26,22 @@ namespace pdflow {
 
 namespace {
 
-constexpr int kTV = 40, kH = 4;
-constexpr int kRV = kTV + 2 * kH;                       // 48 region rows
-constexpr int kPV = kRV / 2;                            // pixel pairs per region column
+constexpr int kH = 4;
 
-// Two shapes: TU = 40 interior columns with 576 threads owning two pairs each,
-// or TU = 34 with 1008 threads owning one pair each (more warps per SM,
-// slightly more halo).
-template <int TU>
+// Three shapes (interior rows TV x columns TU): 40x40 with 576 threads owning
+// two pairs each; 40x34 with 1008 threads owning one pair each (more warps
+// per SM, slightly more halo); 24x24 with 512 threads owning one pair each,
+// small enough (96 KB) for two CTAs per SM, so that one CTA's region load and
+// store overlap the other's iterations at the price of more halo.
+template <int TV, int TU>
 struct Shape {
+    static constexpr int kTV = TV, kRV = TV + 2 * kH, kPV = kRV / 2;   // region rows, pairs per region column
     static constexpr int kTU = TU, kRU = TU + 2 * kH, kPlane = kRV * kRU;
     static constexpr int kCols = TU == 40 ? 2 : 1;      // region columns per thread
     static constexpr int kTY = kRU / kCols;             // columns per sweep
     static constexpr int kThreads = kPV * kTY;
-    static_assert(kTY * kCols == kRU && kThreads <= 1024, "paired tile layout");
+    static constexpr int kBlocksPerSM = TV == 24 ? 2 : 1;
+    static_assert(kTY * kCols == kRU && kThreads <= 1024 && kRV % 2 == 0, "paired tile layout");
 };
 
 enum { T_DU, T_DV, T_DW, T_UA, T_VA, T_WA, T_PD, T_PUU, T_PUV, T_PVU, T_PVV, T_PWU, T_PWV,
@@ -115,10 +118,12 @@ __device__ __forceinline__ void clamp_pd(float& pd)
     if (fabsf(pd) > 1.f) pd = (pd > 1.f) ? 1.f : -1.f;
 }
 
-template <int TU>
-__global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2Args a)
+template <int TV, int TU>
+__global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlocksPerSM)
+    k_iterate_tiles2(Tile2Args a)
 {
-    using S = Shape<TU>;
+    using S = Shape<TV, TU>;
+    constexpr int kTV = S::kTV, kRV = S::kRV, kPV = S::kPV;
     constexpr int kTU = S::kTU, kRU = S::kRU, kPlane = S::kPlane, kCols = S::kCols, kTY = S::kTY;
     extern __shared__ __align__(16) float sm[];
     const size_t po = pair_off(a.g.map, a.g.pstride, blockIdx.y);
@@ -456,41 +461,51 @@ __global__ void __launch_bounds__(Shape<TU>::kThreads, 1) k_iterate_tiles2(Tile2
 
 }  // namespace
 
-cudaError_t prepare_tiles2()
+template <int TV, int TU>
+static cudaError_t prepare_shape()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_iterate_tiles2<40>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(float) * T_NPLANES * Shape<40>::kPlane));
+    cudaError_t e = cudaFuncSetAttribute(k_iterate_tiles2<TV, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float) * T_NPLANES * Shape<TV, TU>::kPlane));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_iterate_tiles2<34>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(float) * T_NPLANES * Shape<34>::kPlane));
+        e = cudaFuncSetAttribute(k_iterate_tiles2<TV, TU>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     return e;
 }
 
-template <int TU>
-static cudaError_t launch_shape(const Tile2Args& a, const LevelGeom& g, cudaStream_t st)
+cudaError_t prepare_tiles2()
 {
-    using S = Shape<TU>;
+    cudaError_t e = prepare_shape<40, 40>();
+    if (e == cudaSuccess) e = prepare_shape<40, 34>();
+    if (e == cudaSuccess) e = prepare_shape<24, 24>();
+    return e;
+}
+
+template <int TV, int TU>
+static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st)
+{
+    using S = Shape<TV, TU>;
+    a.tiles_v = (g.R + TV - 1) / TV;
     dim3 grid(a.tiles_v * ((g.C + TU - 1) / TU), g.pairs);
-    k_iterate_tiles2<TU><<<grid, S::kThreads, sizeof(float) * T_NPLANES * S::kPlane, st>>>(a);
+    k_iterate_tiles2<TV, TU><<<grid, S::kThreads, sizeof(float) * T_NPLANES * S::kPlane, st>>>(a);
     return cudaGetLastError();
 }
 
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // Which region copies use TMA bulk copies, per shape: bit 0 = load, bit 1 =
-// store; index 0 = 40x40 tiles, 1 = 40x34 tiles.  Measured on 64 VGA pairs at
-// 480x640: bulk loads make the 576-thread shape 10 % faster per iteration and
-// the 1008-thread shape 5 % slower (its plain loads already keep 24 loads per
-// thread in flight); bulk stores change neither.
-static int g_copy_mode[2] = {1, 0};
+// store; index 0 = 40x40 tiles, 1 = 40x34 tiles, 2 = 24x24 tiles.  Measured
+// on 64 VGA pairs (whole batched solves, one GB300): bulk loads make the
+// 24x24 shape 9.4 % faster (73.6 -> 66.7 ms), the 40x34 shape 6 % faster
+// (77.3 -> 72.5 ms) and the 40x40 shape 10 % faster per iteration; bulk
+// stores gain nothing on top.
+static int g_copy_mode[3] = {1, 1, 1};
 
 void set_tile_copy_mode(int shape, int mode)
 {
-    if (shape >= 0 && shape < 2) g_copy_mode[shape] = mode & 3;
+    if (shape >= 0 && shape < 3) g_copy_mode[shape] = mode & 3;
 }
 
 cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
-                                  unsigned kk, bool last, cudaStream_t st, bool narrow, unsigned* status)
+                                  unsigned kk, bool last, cudaStream_t st, int shape, unsigned* status)
 {
     Tile2Args a;
     a.g = g;
@@ -501,7 +516,7 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
     a.depth_old = depth_old;
     a.kk = kk;
     a.last = last;
-    a.tiles_v = (g.R + kTV - 1) / kTV;
+    a.tiles_v = 0;   // set per shape
     // bulk copies need every region column start, the region height and the
     // interior height to be multiples of 16 bytes: rows % 4 == 0 (tile and
     // halo sizes are multiples of 4) and 16-byte aligned planes and pair stride
@@ -511,11 +526,16 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
                             L.dct, L.dcu, L.dcv, L.ri, L.rj, L.du_prev, L.dv_prev};
     bool ok = (g.R % 4u) == 0 && (g.pstride % 16u) == 0 && status != nullptr;
     for (const void* q : planes) ok = ok && aligned16(q);
-    const int mode = g_copy_mode[narrow ? 1 : 0];
+    const int mode = g_copy_mode[shape];
     a.bulk = ok && (mode & 1);
     a.bulk_store = ok && (mode & 2);
     a.status = status;
-    return narrow ? launch_shape<34>(a, g, st) : launch_shape<40>(a, g, st);
+    switch (shape) {
+    case 0: return launch_shape<40, 40>(a, g, st);
+    case 1: return launch_shape<40, 34>(a, g, st);
+    case 2: return launch_shape<24, 24>(a, g, st);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace pdflow
