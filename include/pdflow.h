@@ -83,6 +83,15 @@ int pdflow_push_frame_u16(pdflow_solver* s, const uint8_t* intensity, const uint
 /* Same as pdflow_push_frame_u16 with device pointers (no host copy). */
 int pdflow_push_frame_u16_device(pdflow_solver* s, const uint8_t* d_intensity, const uint16_t* d_depth);
 
+/* Same, from an RGB-D camera's raw frames as the reference's live application
+ * converts them (PD_flow_mrpt::CaptureFrame, scene_flow_visualization.cpp:313-323):
+ * row-major RGB888 and uint16 depth in millimetres, converted on the device
+ * bit-exactly as its host loop (gray = 0.299 r + 0.587 g + 0.114 b in double,
+ * each product and sum rounded once, then to float; depth = 0.001f * mm).
+ * rotate180 != 0 stores camera pixel (y, x) at (height-1-y, width-1-x), as that
+ * loop does.  The host variant allocates a device staging buffer on first use. */
+int pdflow_push_frame_rgb8_mm(pdflow_solver* s, const uint8_t* rgb, const uint16_t* depth_mm, int rotate180);
+
 /* Runs the coarse-to-fine solve on the last two pushed frames: replaces
  * PD_flow_opencv::solveSceneFlowGPU (scene_flow_impair.cpp:95-168).  Asynchronous
  * on the solver's stream; pdflow_read_flow or pdflow_synchronize waits. */
@@ -145,6 +154,13 @@ int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float
 /* Pushes raw frames [n][height][width] uint8 / uint16 (as pdflow_push_frame_u16). */
 int pdflow_push_frames_u16(pdflow_solver* s, unsigned n, const uint8_t* intensity, const uint16_t* depth);
 
+/* Pushes RGB888 [n][height][width][3] + millimetre depth [n][height][width]
+ * frames (as pdflow_push_frame_rgb8_mm); host and device-pointer variants. */
+int pdflow_push_frames_rgb8_mm(pdflow_solver* s, unsigned n, const uint8_t* rgb, const uint16_t* depth_mm,
+                               int rotate180);
+int pdflow_push_frames_rgb8_mm_device(pdflow_solver* s, unsigned n, const uint8_t* d_rgb, const uint16_t* d_depth_mm,
+                                      int rotate180);
+
 /* Same with device pointers (contiguous [n][height][width]). */
 int pdflow_push_frames_u16_device(pdflow_solver* s, unsigned n, const uint8_t* d_intensity,
                                   const uint16_t* d_depth);
@@ -205,14 +221,14 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * 2..4 iterations per launch (the iterations between two grid-wide
  * synchronisations), one pixel per lane (form 2) or pixel pairs in packed
  * FP32x2 arithmetic (form 3: 40x40 tiles, 576 threads; form 4: 40x34 tiles,
- * 1008 threads).  pdflow_autotune times every eligible candidate of every
+ * 1008 threads; form 5: 24x24 tiles, 512 threads, two CTAs per SM).  pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The
  * handle's solution state is overwritten (the pushed frames are kept). */
-#define PDFLOW_TUNE_CANDIDATES 11     /* form 0, form 1, forms 2, 3, 4 x {2, 3, 4} iterations per launch */
+#define PDFLOW_TUNE_CANDIDATES 14     /* form 0, form 1, forms 2..5 x {2, 3, 4} iterations per launch */
 typedef struct pdflow_tune_level {
     int form;                         /* chosen form */
-    unsigned iters_per_launch;        /* chosen iterations per launch (form 2) */
+    unsigned iters_per_launch;        /* chosen iterations per launch (forms 2..5) */
     float ms_per_iter[PDFLOW_TUNE_CANDIDATES];   /* per candidate; NaN if not eligible */
 } pdflow_tune_level;
 typedef struct pdflow_tune_report {

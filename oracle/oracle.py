@@ -141,6 +141,19 @@ def decode_frame(intensity: np.ndarray, depth: np.ndarray):
     return I, Z
 
 
+def decode_frame_rgb8_mm(rgb: np.ndarray, depth_mm: np.ndarray, rotate180: bool = False):
+    """The live application's conversion (oracle copy): row-major RGB888 [h, w, 3]
+    and millimetre depth [h, w] -> column-major float intensity and metres."""
+    h, w = depth_mm.shape
+    I = np.zeros(w * h, np.float32)
+    Z = np.zeros(w * h, np.float32)
+    f = lib().or_decode_frame_rgb8_mm
+    f.restype = None
+    f(ctypes.c_uint(w), ctypes.c_uint(h), _ptr(np.ascontiguousarray(rgb, np.uint8)),
+      _ptr(np.ascontiguousarray(depth_mm, np.uint16)), ctypes.c_int(int(rotate180)), _ptr(I), _ptr(Z))
+    return I, Z
+
+
 def energy(R: int, C: int, old: tuple, new: tuple, du, dv, dw, mu: float = 75.0, lambda_i: float = 0.04,
            lambda_d: float = 0.35, precision: str = "f64") -> float:
     """Energy of a level solution (or_energy, pdflow_oracle.c): `old`/`new` are

@@ -858,4 +858,27 @@ void or_decode_frame(unsigned width, unsigned height, const uint8_t* img_rowmajo
             Z_colmajor[v + u * height] = (float)depth_rowmajor[(size_t)v * width + u] * scale;
         }
 }
+
+/* The live application's frame conversion (PD_flow_mrpt::CaptureFrame,
+ * scene_flow_visualization.cpp:313-323): camera pixel (y, x) of a row-major
+ * RGB888 + millimetre depth frame becomes
+ *   colour(yc, xc) = (float)(0.299*r + 0.587*g + 0.114*b)   (double arithmetic)
+ *   depth(yc, xc)  = 0.001f * mm                              (float)
+ * at yc = height-1-y, xc = width-1-x (its loops walk the camera rows and
+ * columns forward while counting yc and xc down; rotate180 = 0 stores (y, x)
+ * in place), packed column-major as Eigen's MatrixXf::data() hands it to
+ * copyNewFrames (scene_flow_visualization.cpp:115). */
+void or_decode_frame_rgb8_mm(unsigned width, unsigned height, const uint8_t* rgb_rowmajor,
+                             const uint16_t* depth_mm_rowmajor, int rotate180, float* I_colmajor, float* Z_colmajor)
+{
+    for (unsigned y = 0; y < height; ++y)
+        for (unsigned x = 0; x < width; ++x) {
+            const size_t i = (size_t)y * width + x;
+            const unsigned yc = rotate180 ? height - 1 - y : y, xc = rotate180 ? width - 1 - x : x;
+            const uint8_t* p = rgb_rowmajor + 3 * i;
+            const double gray = 0.299 * p[0] + 0.587 * p[1] + 0.114 * p[2];
+            I_colmajor[yc + xc * height] = (float)gray;
+            Z_colmajor[yc + xc * height] = 0.001f * (float)depth_mm_rowmajor[i];
+        }
+}
 #endif

@@ -61,6 +61,40 @@ __global__ void __launch_bounds__(1024) k_decode_u16(const uint8_t* __restrict__
     }
 }
 
+// Row-major RGB888 + uint16 millimetre depth -> column-major level 0 with the
+// live application's conversion (gray_rgb, decode_depth_mm).  rotate180: its
+// camera loop (scene_flow_visualization.cpp:313-323) stores camera pixel
+// (y, x) at row H-1-y, column W-1-x.
+__global__ void __launch_bounds__(1024) k_decode_rgb8_mm(const uint8_t* __restrict__ rgb,
+                                                         const uint16_t* __restrict__ depth, unsigned W, unsigned H,
+                                                         PyrLevel out, float fovh, size_t pstride,
+                                                         const unsigned* __restrict__ map, int rotate180)
+{
+    rgb += (size_t)blockIdx.z * W * H * 3;
+    depth += (size_t)blockIdx.z * W * H;
+    out = at(out, pair_off(map, pstride, blockIdx.z));
+    __shared__ float sc[32][33];
+    __shared__ float sz[32][33];
+    const unsigned x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    {
+        const unsigned x = x0 + threadIdx.x, y = y0 + threadIdx.y;   // stored (row y, column x)
+        if (x < W && y < H) {
+            const size_t i = rotate180 ? (size_t)(H - 1 - y) * W + (W - 1 - x) : (size_t)y * W + x;
+            sc[threadIdx.y][threadIdx.x] = gray_rgb(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+            sz[threadIdx.y][threadIdx.x] = decode_depth_mm(depth[i]);
+        }
+    }
+    __syncthreads();
+    const unsigned v = y0 + threadIdx.x, u = x0 + threadIdx.y;  // writes walk along v
+    if (u < W && v < H) {
+        const unsigned idx = v + u * H;
+        const float z = sz[threadIdx.x][threadIdx.y];
+        out.col[idx] = sc[threadIdx.x][threadIdx.y];
+        out.dep[idx] = z;
+        write_xy(out, H, W, v, u, idx, z, fovh);
+    }
+}
+
 __global__ void k_pyr_level0(const float* __restrict__ I, const float* __restrict__ Z, unsigned R, unsigned C,
                              PyrLevel out, float fovh, size_t pstride, const unsigned* __restrict__ map)
 {
@@ -626,6 +660,14 @@ cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigne
 {
     dim3 grid((W + 31) / 32, (H + 31) / 32, pairs), block(32, 32);
     k_decode_u16<<<grid, block, 0, st>>>(img, depth, W, H, out, fovh, pstride, map);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_decode_rgb8_mm(const uint8_t* rgb, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
+                                  float fovh, unsigned pairs, size_t pstride, cudaStream_t st, int rotate180)
+{
+    dim3 grid((W + 31) / 32, (H + 31) / 32, pairs), block(32, 32);
+    k_decode_rgb8_mm<<<grid, block, 0, st>>>(rgb, depth, W, H, out, fovh, pstride, nullptr, rotate180);
     return cudaGetLastError();
 }
 

@@ -108,6 +108,9 @@ struct Params {
 cudaError_t launch_decode_u16(const uint8_t* img, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
                               float fovh, unsigned pairs, size_t pstride, cudaStream_t st,
                               const unsigned* map = nullptr);
+// RGB888 [pairs][H][W][3] + millimetre depth [pairs][H][W] (the live application's conversion).
+cudaError_t launch_decode_rgb8_mm(const uint8_t* rgb, const uint16_t* depth, unsigned W, unsigned H, PyrLevel out,
+                                  float fovh, unsigned pairs, size_t pstride, cudaStream_t st, int rotate180);
 cudaError_t launch_pyr_level0(const float* I, const float* Z, unsigned R, unsigned C, PyrLevel out, float fovh,
                               unsigned pairs, size_t pstride, cudaStream_t st, const unsigned* map = nullptr);
 cudaError_t launch_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, float fovh, unsigned pairs,

@@ -42,6 +42,18 @@ __device__ __forceinline__ float gmask(int k, int l)
 // (scene_flow_impair.cpp:242, :269 via OpenCV convertTo). One rounding.
 __device__ __forceinline__ float decode_depth(unsigned short d) { return __fmul_rn(float(d), 0.0002f); }
 
+// The live application's conversion of an RGB-D camera's frames
+// (scene_flow_visualization.cpp:320-321): gray = 0.299 r + 0.587 g + 0.114 b
+// evaluated in double, each product and sum rounded once, then rounded to
+// float; depth = 0.001f * millimetres in float.
+__device__ __forceinline__ float gray_rgb(unsigned r, unsigned g, unsigned b)
+{
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(0.299, double(r)), __dmul_rn(0.587, double(g))),
+                               __dmul_rn(0.114, double(b)));
+    return __double2float_rn(s);
+}
+__device__ __forceinline__ float decode_depth_mm(unsigned short d) { return __fmul_rn(0.001f, float(d)); }
+
 // Focal factor 2*tan(fovh/2)/cols of computePyramidLevel (pdflow_cudalib.cu:428)
 // and computeMotionField (:1152).
 __device__ __forceinline__ float inv_focal(float fovh, unsigned cols)

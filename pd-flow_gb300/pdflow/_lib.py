@@ -32,7 +32,7 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
-TUNE_CANDIDATES = 11   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2/3/4 x {2, 3, 4} iterations per launch
+TUNE_CANDIDATES = 14   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..5 x {2, 3, 4} iterations per launch
 
 
 class TuneLevel(ctypes.Structure):
@@ -112,6 +112,9 @@ _SIGNATURES = {
     "pdflow_destroy": (ctypes.c_int, [vp]),
     "pdflow_push_frame": (ctypes.c_int, [vp, vp, vp]),
     "pdflow_push_frame_u16": (ctypes.c_int, [vp, vp, vp]),
+    "pdflow_push_frame_rgb8_mm": (ctypes.c_int, [vp, vp, vp, ctypes.c_int]),
+    "pdflow_push_frames_rgb8_mm": (ctypes.c_int, [vp, u32, vp, vp, ctypes.c_int]),
+    "pdflow_push_frames_rgb8_mm_device": (ctypes.c_int, [vp, u32, vp, vp, ctypes.c_int]),
     "pdflow_push_frame_u16_device": (ctypes.c_int, [vp, vp, vp]),
     "pdflow_solve": (ctypes.c_int, [vp]),
     "pdflow_read_flow": (ctypes.c_int, [vp, vp, vp, vp]),
@@ -308,7 +311,7 @@ class Solver(_Extras):
     freeGPUMemory."""
 
     def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 4):
+                 use_graph: bool = True, iteration_form: int = 5):
         self.rows, self.width, self.height = rows, width, height
         self.cols = rows * 320 // 240
         self.params = params
@@ -345,6 +348,17 @@ class Solver(_Extras):
         if i8.shape != (self.height, self.width) or z16.shape != i8.shape:
             raise ValueError("frame size does not match the solver")
         check(load().pdflow_push_frame_u16(self._h, _ptr(i8), _ptr(z16)), "pdflow_push_frame_u16")
+
+    def push_rgb(self, rgb: np.ndarray, depth_mm: np.ndarray, rotate180: bool = False):
+        """Push an RGB-D camera frame: row-major RGB888 [h, w, 3] and uint16
+        millimetre depth [h, w], converted on the GPU as the reference's live
+        application does (pdflow_push_frame_rgb8_mm)."""
+        c8 = np.ascontiguousarray(rgb, np.uint8)
+        z16 = np.ascontiguousarray(depth_mm, np.uint16)
+        if c8.shape != (self.height, self.width, 3) or z16.shape != (self.height, self.width):
+            raise ValueError("frame size does not match the solver")
+        check(load().pdflow_push_frame_rgb8_mm(self._h, _ptr(c8), _ptr(z16), int(rotate180)),
+              "pdflow_push_frame_rgb8_mm")
 
     def loadRGBDFrames(self, i1, z1, i2, z2):
         """Push two raw frames (the reference loads two PNGs, scene_flow_impair.cpp:218-277)."""
@@ -432,7 +446,7 @@ class BatchSolver(_Extras):
     a camera stream that keeps its previous frame on the device."""
 
     def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 4):
+                 use_graph: bool = True, iteration_form: int = 5):
         lib = load()
         self.rows, self.width, self.height, self.max_pairs = rows, width, height, max_pairs
         self.cols = rows * 320 // 240
@@ -457,6 +471,17 @@ class BatchSolver(_Extras):
         if i8.shape != (n, self.height, self.width) or z16.shape != i8.shape:
             raise ValueError("expected stacks [n, height, width]")
         check(load().pdflow_push_frames_u16(self._h, n, _ptr(i8), _ptr(z16)), "pdflow_push_frames_u16")
+
+    def push_rgb(self, rgb: np.ndarray, depth_mm: np.ndarray, rotate180: bool = False):
+        """Push stacks [n, height, width, 3] RGB888 / [n, height, width] millimetre
+        depth (pdflow_push_frames_rgb8_mm)."""
+        c8 = np.ascontiguousarray(rgb, np.uint8)
+        z16 = np.ascontiguousarray(depth_mm, np.uint16)
+        n = z16.shape[0]
+        if c8.shape != (n, self.height, self.width, 3) or z16.shape != (n, self.height, self.width):
+            raise ValueError("expected stacks [n, height, width, 3] and [n, height, width]")
+        check(load().pdflow_push_frames_rgb8_mm(self._h, n, _ptr(c8), _ptr(z16), int(rotate180)),
+              "pdflow_push_frames_rgb8_mm")
 
     def push_raw_device(self, n: int, d_intensity: int, d_depth: int):
         check(load().pdflow_push_frames_u16_device(self._h, n, ctypes.c_void_p(d_intensity),

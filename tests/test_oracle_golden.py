@@ -147,3 +147,25 @@ def test_median_sorting_network_sorts_every_zero_one_input():
             if keys[b] < keys[a]:
                 keys[a], keys[b] = keys[b], keys[a]
         assert [i for _, i in keys] == sorted(range(9), key=lambda i: (vals[i], i))
+
+
+def test_live_app_rgb_decode_every_value():
+    """The oracle's RGB888 + millimetre conversion equals a numpy restatement of
+    scene_flow_visualization.cpp:320-321 for every RGB triple and every depth
+    value, and the 180-degree storage order of its camera loop."""
+    k = np.arange(1 << 24, dtype=np.uint32)
+    rgb = np.stack([k & 255, (k >> 8) & 255, k >> 16], axis=-1).astype(np.uint8).reshape(4096, 4096, 3)
+    mm = (k & 0xFFFF).astype(np.uint16).reshape(4096, 4096)
+    I, Z = oracle.decode_frame_rgb8_mm(rgb, mm, False)
+    c = rgb.astype(np.float64)
+    gray = ((0.299 * c[..., 0] + 0.587 * c[..., 1]) + 0.114 * c[..., 2]).astype(np.float32)
+    depth = np.float32(0.001) * mm.astype(np.float32)
+    assert np.array_equal(I.view(np.uint32), gray.T.ravel().view(np.uint32))
+    assert np.array_equal(Z.view(np.uint32), depth.T.ravel().view(np.uint32))
+    # hand-checked values: white stays 255, 1000 mm is 1 m
+    assert I[0] == 0.0 and gray[4095, 4095] == np.float32(255.0) and depth[0, 1000] == np.float32(1.0)
+    small = rgb[:5, :7]
+    I0, Z0 = oracle.decode_frame_rgb8_mm(small, mm[:5, :7], False)
+    I1, Z1 = oracle.decode_frame_rgb8_mm(small, mm[:5, :7], True)
+    assert np.array_equal(I1.reshape(7, 5), I0.reshape(7, 5)[::-1, ::-1])
+    assert np.array_equal(Z1.reshape(7, 5), Z0.reshape(7, 5)[::-1, ::-1])
