@@ -188,15 +188,17 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per pixel-iteration of the tile iteration kernel, from the
-    committed ncu summary (the `bytes_per_px_iter:` line), else None."""
+def profiled_traffic(form):
+    """DRAM bytes per pixel-iteration of the 480x640 tile launch of iteration
+    form `form`, from the committed ncu summary (`bytes_per_px_iter_formN:`
+    lines), else None."""
+    key = f"bytes_per_px_iter_form{form}:"
     try:
-        with open(os.path.join(ROOT, "profiles", "k_iterate_tiles2_vga_batch16.md")) as f:
+        with open(os.path.join(ROOT, "profiles", "k_iterate_tiles2_forms_vga_batch16_480x640.md")) as f:
             for line in f:
-                if line.startswith("bytes_per_px_iter:"):
-                    return {"bytes_per_px_iter": float(line.split(":")[1])}
-    except (OSError, ValueError):
+                if line.startswith(key):
+                    return {"bytes_per_px_iter": float(line.split(":")[1]), "form": form}
+    except OSError:
         pass
     return None
 
@@ -369,24 +371,27 @@ def ours(args):
     # ---------------- roofline: the finest level's iterations ----------------
     hbm_peak, peak_kind = measured_peaks()
     R_f, C_f = ROWS, ROWS * 4 // 3
-    iters = 10
+    iters = 24                                                 # whole launches of 2, 3 or 4 iterations
     ms = ctypes.c_float()
     with torch.cuda.stream(stream):
         _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
         _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
     alg_bytes = ALG_BYTES_PER_PX_ITER * B * R_f * C_f          # per iteration
     achieved = alg_bytes / (ms.value / iters / 1000.0) / 1e9
-    trf = profiled_traffic()
+    fine_form = tune[5]["form"] if len(tune) > 5 else 5
+    fine_kk = tune[5]["iters_per_launch"] if len(tune) > 5 else 4
+    trf = profiled_traffic(fine_form)
     traffic = None
     if trf and trf.get("bytes_per_px_iter"):
-        # DRAM bytes per iteration, scaled from a 16-pair capture at 240x320
-        # (traffic per pixel-iteration does not depend on the batch size)
+        # DRAM bytes per iteration, scaled from a 16-pair capture of the same
+        # level and form (traffic per pixel-iteration does not depend on the
+        # batch size: each launch reads the level's planes once)
         traffic = float(trf["bytes_per_px_iter"]) * B * R_f * C_f
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": traffic, "traffic_basis": "DRAM bytes per iteration of the timed level (scaled ncu capture)",
                 "peak_kind": peak_kind,
-                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles2, autotuned form and "
-                          "iterations per launch)",
+                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles2, autotuned form "
+                          f"{fine_form}, {fine_kk} iterations per launch)",
                 "algorithmic_bytes_per_px_iter": ALG_BYTES_PER_PX_ITER,
                 "ms_per_iteration": ms.value / iters}
 

@@ -221,11 +221,12 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * 2..4 iterations per launch (the iterations between two grid-wide
  * synchronisations), one pixel per lane (form 2) or pixel pairs in packed
  * FP32x2 arithmetic (form 3: 40x40 tiles, 576 threads; form 4: 40x34 tiles,
- * 1008 threads; form 5: 24x24 tiles, 512 threads, two CTAs per SM).  pdflow_autotune times every eligible candidate of every
+ * 1008 threads; form 5: 24x24 tiles, 512 threads, two CTAs per SM; form 6:
+ * 24x28 tiles, 288 threads owning two pairs each, two CTAs per SM).  pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The
  * handle's solution state is overwritten (the pushed frames are kept). */
-#define PDFLOW_TUNE_CANDIDATES 14     /* form 0, form 1, forms 2..5 x {2, 3, 4} iterations per launch */
+#define PDFLOW_TUNE_CANDIDATES 17     /* form 0, form 1, forms 2..6 x {2, 3, 4} iterations per launch */
 typedef struct pdflow_tune_level {
     int form;                         /* chosen form */
     unsigned iters_per_launch;        /* chosen iterations per launch (forms 2..5) */

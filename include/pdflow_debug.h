@@ -30,8 +30,9 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
  * iterations per launch; 24x24 tiles, one pixel pair per thread in packed
  * FP32x2 arithmetic, two CTAs per SM so that one CTA's region load and store
  * overlap the other's iterations), a single pair's smaller levels as one
- * launch per level; 4 = the same with 40x34 tiles (1008 threads, one CTA per
- * SM); 3 = the same with 40x40 tiles and two pairs per thread; 2 = one pixel
+ * launch per level; 6 = the same with 24x28 tiles (288 threads owning two
+ * pairs each, two CTAs per SM); 4 = the same with 40x34 tiles (1008 threads,
+ * one CTA per SM); 3 = the same with 40x40 tiles and two pairs per thread; 2 = one pixel
  * per lane; 1 = one launch per level (slab-persistent kernel; batches use two
  * kernels per iteration for the large levels); 0 = two kernels per iteration
  * (the reference's launch structure with gradient+dual and divergence+primal
@@ -71,7 +72,7 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
 /* How the paired tile kernels move a tile's region between HBM and shared
  * memory (process-wide; graphs captured afterwards use it): shape 0 = 40x40
  * tiles (iteration form 3), 1 = 40x34 tiles (form 4), 2 = 24x24 tiles
- * (form 5); mode bit 0 = TMA bulk
+ * (form 5), 3 = 24x28 tiles (form 6); mode bit 0 = TMA bulk
  * copies for the region load, bit 1 = for the interior store, else plain
  * loads/stores.  Levels whose row count is not a multiple of 4 always use
  * plain loads and stores.  All modes give the same bits. */

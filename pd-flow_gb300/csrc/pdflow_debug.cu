@@ -134,7 +134,7 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 
 int pdflow_set_iteration_form(pdflow_solver* s, int form)
 {
-    if (!s || form < 0 || form > 5) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..5");
+    if (!s || form < 0 || form > 6) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..6");
     if (s->iter_form != form) {
         cudaStreamSynchronize(s->stream);
         s->iter_form = form;   // graphs are cached per iteration form
@@ -224,7 +224,7 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
 
 int pdflow_set_tile_copy_mode(int shape, int mode)
 {
-    if (shape < 0 || shape > 2 || mode < 0 || mode > 3) return fail(PDFLOW_ERR_ARG, "shape 0..2, mode 0..3");
+    if (shape < 0 || shape > 3 || mode < 0 || mode > 3) return fail(PDFLOW_ERR_ARG, "shape 0..3, mode 0..3");
     set_tile_copy_mode(shape, mode);
     return PDFLOW_OK;
 }

@@ -204,7 +204,7 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
     }
     const bool paired = tiles && form >= 3;
-    const int shape = form - 3;   // 40x40, 40x34 or 24x24 tiles
+    const int shape = form - 3;   // 40x40, 40x34, 24x24 or 24x28 tiles
     if (tiles) {
         State cur = s->S;
         State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],

@@ -28,19 +28,20 @@ namespace {
 
 constexpr int kH = 4;
 
-// Three shapes (interior rows TV x columns TU): 40x40 with 576 threads owning
+// Four shapes (interior rows TV x columns TU): 40x40 with 576 threads owning
 // two pairs each; 40x34 with 1008 threads owning one pair each (more warps
 // per SM, slightly more halo); 24x24 with 512 threads owning one pair each,
 // small enough (96 KB) for two CTAs per SM, so that one CTA's region load and
-// store overlap the other's iterations at the price of more halo.
+// store overlap the other's iterations at the price of more halo; 24x28 with
+// 288 threads owning two pairs each, two CTAs per SM (108 KB each).
 template <int TV, int TU>
 struct Shape {
     static constexpr int kTV = TV, kRV = TV + 2 * kH, kPV = kRV / 2;   // region rows, pairs per region column
     static constexpr int kTU = TU, kRU = TU + 2 * kH, kPlane = kRV * kRU;
-    static constexpr int kCols = TU == 40 ? 2 : 1;      // region columns per thread
+    static constexpr int kCols = (TU == 40 || TU == 28) ? 2 : 1;   // region columns per thread
     static constexpr int kTY = kRU / kCols;             // columns per sweep
     static constexpr int kThreads = kPV * kTY;
-    static constexpr int kBlocksPerSM = TV == 24 ? 2 : 1;
+    static constexpr int kBlocksPerSM = TV == 24 ? 2 : 1;           // CTAs per SM the registers allow
     static_assert(kTY * kCols == kRU && kThreads <= 1024 && kRV % 2 == 0, "paired tile layout");
 };
 
@@ -476,6 +477,7 @@ cudaError_t prepare_tiles2()
     cudaError_t e = prepare_shape<40, 40>();
     if (e == cudaSuccess) e = prepare_shape<40, 34>();
     if (e == cudaSuccess) e = prepare_shape<24, 24>();
+    if (e == cudaSuccess) e = prepare_shape<24, 28>();
     return e;
 }
 
@@ -492,16 +494,16 @@ static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // Which region copies use TMA bulk copies, per shape: bit 0 = load, bit 1 =
-// store; index 0 = 40x40 tiles, 1 = 40x34 tiles, 2 = 24x24 tiles.  Measured
+// store; index 0 = 40x40 tiles, 1 = 40x34 tiles, 2 = 24x24, 3 = 24x28.  Measured
 // on 64 VGA pairs (whole batched solves, one GB300): bulk loads make the
 // 24x24 shape 9.4 % faster (73.6 -> 66.7 ms), the 40x34 shape 6 % faster
 // (77.3 -> 72.5 ms) and the 40x40 shape 10 % faster per iteration; bulk
 // stores gain nothing on top.
-static int g_copy_mode[3] = {1, 1, 1};
+static int g_copy_mode[4] = {1, 1, 1, 1};
 
 void set_tile_copy_mode(int shape, int mode)
 {
-    if (shape >= 0 && shape < 3) g_copy_mode[shape] = mode & 3;
+    if (shape >= 0 && shape < 4) g_copy_mode[shape] = mode & 3;
 }
 
 cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
@@ -534,6 +536,7 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
     case 0: return launch_shape<40, 40>(a, g, st);
     case 1: return launch_shape<40, 34>(a, g, st);
     case 2: return launch_shape<24, 24>(a, g, st);
+    case 3: return launch_shape<24, 28>(a, g, st);
     default: return cudaErrorInvalidValue;
     }
 }

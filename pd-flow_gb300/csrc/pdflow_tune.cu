@@ -19,7 +19,7 @@ struct Candidate {
 };
 constexpr Candidate kCandidates[PDFLOW_TUNE_CANDIDATES] = {{0, 0}, {1, 0}, {2, 2}, {2, 3}, {2, 4}, {3, 2},
                                                             {3, 3}, {3, 4}, {4, 2}, {4, 3}, {4, 4}, {5, 2},
-                                                            {5, 3}, {5, 4}};
+                                                            {5, 3}, {5, 4}, {6, 2}, {6, 3}, {6, 4}};
 
 void drop_graphs(pdflow_solver* s)
 {
@@ -35,8 +35,8 @@ extern "C" {
 
 int pdflow_set_level_form(pdflow_solver* s, unsigned level, int form, unsigned iters_per_launch)
 {
-    if (!s || level >= 8 || form < -1 || form > 5 || iters_per_launch > 4) {
-        set_last_error("bad argument (form -1..5, level < 8, iterations per launch 0..4)");
+    if (!s || level >= 8 || form < -1 || form > 6 || iters_per_launch > 4) {
+        set_last_error("bad argument (form -1..6, level < 8, iterations per launch 0..4)");
         return PDFLOW_ERR_ARG;
     }
     drop_graphs(s);

@@ -32,7 +32,7 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
-TUNE_CANDIDATES = 14   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..5 x {2, 3, 4} iterations per launch
+TUNE_CANDIDATES = 17   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..6 x {2, 3, 4} iterations per launch
 
 
 class TuneLevel(ctypes.Structure):

@@ -22,7 +22,7 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     rep = b.autotune(3)
     assert len(rep) == 5
     for lvl in rep:
-        assert lvl["form"] in (0, 1, 2, 3, 4, 5)
+        assert lvl["form"] in (0, 1, 2, 3, 4, 5, 6)
         assert lvl["ms_per_iter"][0] is not None
     b.solve(3)
     got = b.read_flow(3)
@@ -39,10 +39,10 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     b.close()
 
 
-DEFAULT_COPY_MODE = {3: 1, 4: 1, 5: 1}   # the library's defaults (pdflow_tiles2.cu)
+DEFAULT_COPY_MODE = {3: 1, 4: 1, 5: 1, 6: 1}   # the library's defaults (pdflow_tiles2.cu)
 
 
-@pytest.mark.parametrize("form", [3, 4, 5])
+@pytest.mark.parametrize("form", [3, 4, 5, 6])
 def test_tile_copy_modes_give_the_same_bits(built_lib, form):
     import ctypes
     from pdflow import _lib
