@@ -440,9 +440,11 @@ __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* dep
 //
 // Stable sort of up to 9 samples (the reference's bubbleSortDev,
 // pdflow_cudalib.cu:1457-1473, swaps only on a strict '>', so equal values
-// keep their input order) as a 28-comparator sorting network on (value, input
-// index) keys: Batcher's odd-even merge network for 16 inputs restricted to 9,
-// which sorts every 0/1 input and hence every input.  Missing samples (n < 9)
+// keep their input order) as a 25-comparator sorting network on (value, input
+// index) keys (sort each triple, sort the columns of the 3x3 array, five
+// exchanges), which sorts every 0/1 input and hence every input; with the
+// index as tie-break the keys are distinct, so any sorting network yields
+// the stable order.  Missing samples (n < 9)
 // enter as (+inf, index >= n) and sort last.  Then the cumulative weights are
 // summed in sorted order, as the reference does, and the bracketing samples
 // are interpolated; the result and the selected index are the reference's bit
@@ -472,11 +474,13 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
         sw[i] = in ? w[i] : 0.f;
         id[i] = i;
     }
-    constexpr int kNet[28][2] = {{0, 1}, {2, 3}, {0, 2}, {1, 3}, {1, 2}, {4, 5}, {6, 7}, {4, 6}, {5, 7}, {5, 6},
-                                 {0, 4}, {2, 6}, {2, 4}, {1, 5}, {3, 7}, {3, 5}, {1, 2}, {3, 4}, {5, 6}, {0, 8},
-                                 {4, 8}, {2, 4}, {6, 8}, {3, 5}, {1, 2}, {3, 4}, {5, 6}, {7, 8}};
+    // 25 comparators: sort the triples (0,1,2), (3,4,5), (6,7,8), sort the
+    // columns of the resulting 3x3 array, then the last five exchanges
+    constexpr int kNet[25][2] = {{0, 1}, {3, 4}, {6, 7}, {1, 2}, {4, 5}, {7, 8}, {0, 1}, {3, 4}, {6, 7},
+                                 {0, 3}, {3, 6}, {0, 3}, {1, 4}, {4, 7}, {1, 4}, {2, 5}, {5, 8}, {2, 5},
+                                 {1, 3}, {5, 7}, {2, 6}, {4, 6}, {2, 4}, {2, 3}, {5, 6}};
 #pragma unroll
-    for (int c = 0; c < 28; ++c) {
+    for (int c = 0; c < 25; ++c) {
         const int a = kNet[c][0], b = kNet[c][1];
         cmp_swap(sf[a], sw[a], id[a], sf[b], sw[b], id[b]);
     }

@@ -121,17 +121,17 @@ def test_oracle_level_state_tracks_reference(golden_qvga, oracle_r60_dumps, fiel
 
 
 def test_median_sorting_network_sorts_every_zero_one_input():
-    """The 9-input comparator network of k_median (Batcher's odd-even merge
-    network for 16 inputs restricted to 9) sorts all 512 zero-one inputs, so
+    """The 9-input comparator network of k_median (25 comparators: the
+    triples, the columns of the 3x3 array, five exchanges) sorts all 512 zero-one inputs, so
     by the 0-1 principle it sorts every input; with (value, input index) keys
     it reproduces the stable order of the reference's bubble sort."""
     import itertools
     import re
     src = open(os.path.join(os.path.dirname(__file__), "..", "pd-flow_gb300", "csrc", "pdflow_kernels.cu")).read()
-    body = src[src.index("kNet[28][2] = {"):]
+    body = src[src.index("kNet[25][2] = {"):]
     body = body[:body.index("};")]
     net = [tuple(map(int, m)) for m in re.findall(r"\{(\d+), (\d+)\}", body)]
-    assert len(net) == 28
+    assert len(net) == 25
     for bits in itertools.product((0, 1), repeat=9):
         x = list(bits)
         for a, b in net:
