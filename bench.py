@@ -368,6 +368,28 @@ def ours(args):
     torch.cuda.synchronize()
     batched_plain = {"pairs_s": B * max(3, K // 2) / (ta.elapsed_time(tb) / 1000.0), "epe_vs_plain_mm": 0.0}
 
+    # the learned warm start with the finer levels' iterations halved (the
+    # schedule's nominal setting), same handle, frames and fallback rule
+    half = 0.5
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            push()
+            b.solve_learned(B, net, half, margin)
+        b.synchronize()
+        ta.record(stream)
+        fb_half = 0
+        for _ in range(max(3, K // 2)):
+            push()
+            fb_half += b.solve_learned(B, net, half, margin)["fallbacks"]
+        tb.record(stream)
+    torch.cuda.synchronize()
+    f_half = b.read_flow(B)
+    learned_half = {"iter_scale": half, "pairs_s": B * max(3, K // 2) / (ta.elapsed_time(tb) / 1000.0),
+                    "fallbacks_per_step": fb_half / max(3, K // 2),
+                    "epe_vs_plain_mm": float(epe(f_half, plain_b, valid).mean() * 1e3),
+                    "epe_vs_ground_truth_mm": float(epe(f_half, gt, valid).mean() * 1e3),
+                    "energy_ratio_to_plain": float((b.energy(B) / e_plain).mean())}
+
     # ---------------- roofline: the finest level's iterations ----------------
     hbm_peak, peak_kind = measured_peaks()
     R_f, C_f = ROWS, ROWS * 4 // 3
@@ -484,7 +506,8 @@ def ours(args):
             "accuracy": accuracy,
             "batched": {"pairs_s": value, "p50_ms_per_batch": statistics.median(step_ms),
                         "p99_ms_per_batch": float(np.quantile(step_ms, 0.99))},
-            "batched_plain": batched_plain, "mixed_batch": mixed, "plain": plain,
+            "batched_plain": batched_plain, "learned_half_iterations": learned_half, "mixed_batch": mixed,
+            "plain": plain,
             "speedup_vs_plain_single": value / plain["pairs_s"],
             "p99_ms": serving["vga_p99_ms"] if serving and "vga_p99_ms" in serving else None,
             "serving": serving, "autotune": tune, "e2e": e2e, "roofline": roofline,
