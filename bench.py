@@ -594,7 +594,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--iter-scale", type=float, default=0.75)
     ap.add_argument("--energy-margin", type=float, default=0.01)
-    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

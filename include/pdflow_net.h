@@ -9,7 +9,8 @@
  * pyramid level to that level's flow.  pdflow_solve_batch_learned starts the
  * coarse-to-fine solve at the 60x80 level from the prediction, with scaled
  * iteration counts, and falls back to the plain solve per pair when the
- * energy rule rejects the prediction.  The network is trained by the same
+ * energy rule rejects the prediction (a rejected pair continues from the
+ * plain 60x80 solution, so its result is the plain solve's bit for bit).  The network is trained by the same
  * library (pdflow_net_train_step) on flows the plain solver produces.
  */
 #ifndef PDFLOW_NET_H
@@ -65,7 +66,7 @@ typedef struct pdflow_learned_opts {
 } pdflow_learned_opts;
 
 typedef struct pdflow_learned_report {
-    unsigned fallbacks;      /* pairs re-solved by the plain solver */
+    unsigned fallbacks;      /* pairs finished by the plain schedule (from the plain 60x80 solution) */
     float max_energy_ratio;  /* max over pairs of E(learned) / E(plain) at the seed level */
 } pdflow_learned_report;
 

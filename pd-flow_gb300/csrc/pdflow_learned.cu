@@ -1,10 +1,13 @@
 // Learned warm start of a batched solve (include/pdflow_net.h).
 //
-// One CUDA graph per (pair count, iteration scale, slot addressing) runs the
-// plain schedule to the 60x80 level with its energy, the network on that
-// level's images, and the warm-started schedule from the 60x80 level with its
-// own energy; the host then compares the two energies per pair and re-solves
-// the rejected pairs with the plain schedule.
+// A first CUDA graph per (pair count, iteration scale, slot addressing) runs
+// the plain schedule to the 60x80 level with its energy, keeps that level's
+// plain solution, runs the network on the level's images and the 60x80 level
+// again from the network's prediction with its own energy.  The host compares
+// the two energies per pair; a second graph continues the accepted pairs with
+// the warm-started schedule from 120x160 on, a third puts the kept plain
+// 60x80 solution back for the rejected pairs and continues them with the plain
+// schedule, which makes them the plain solve bit for bit.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -46,6 +49,31 @@ __global__ void k_seed_labels(LevelSol sol, unsigned R, unsigned s, size_t pstri
     o[2 * kSeedN + q] = float(w * inv);
 }
 
+// Saves (save = true) or restores the 10 solution planes (du, dv, dw and the
+// 7 duals) of the 60x80 level of the mapped pairs to / from keep[slot][10][n].
+__global__ void k_sol_keep(LevelSol sol, float* __restrict__ keep, unsigned n, size_t pstride,
+                           const unsigned* __restrict__ map, bool save)
+{
+    const unsigned slot = map ? (__ldg(map + blockIdx.y) & kMapSlotMask) : blockIdx.y;
+    sol = at(sol, pair_off(map, pstride, blockIdx.y));
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* k = keep + size_t(slot) * 10 * n;
+    float* p[10] = {sol.du, sol.dv, sol.dw, sol.pd, sol.puu, sol.puv, sol.pvu, sol.pvv, sol.pwu, sol.pwv};
+#pragma unroll
+    for (int c = 0; c < 10; ++c) {
+        if (save) k[size_t(c) * n + i] = p[c][i];
+        else p[c][i] = k[size_t(c) * n + i];
+    }
+}
+
+cudaError_t launch_sol_keep(pdflow_solver* s, unsigned pairs, const unsigned* map, bool save, cudaStream_t st)
+{
+    dim3 grid((kSeedN + 255) / 256, pairs);
+    k_sol_keep<<<grid, 256, 0, st>>>(s->sol, s->sol_keep, kSeedN, s->pair_stride, map, save);
+    return cudaGetLastError();
+}
+
 struct LearnedCtx {
     pdflow_net* net;
     float iter_scale;
@@ -65,6 +93,9 @@ int learned_enqueue(pdflow_solver* s, cudaStream_t st, unsigned pairs, const voi
     int rc = enqueue_solve(s, st, pairs, plain);
     if (rc) return rc;
     total += s->launches;
+    if (cudaError_t e = launch_sol_keep(s, pairs, map, true, st))
+        return set_error_code(PDFLOW_ERR_CUDA, "keep the plain 60x80 solution", e);
+    total += 1;
 
     unsigned li;
     level_geom(s, kSeedLevel, &li, pairs);
@@ -79,6 +110,7 @@ int learned_enqueue(pdflow_solver* s, cudaStream_t st, unsigned pairs, const voi
 
     SolvePlan warm;
     warm.first = kSeedLevel;
+    warm.last = kSeedLevel;
     warm.seed = s->seed;
     warm.iter_scale = c.iter_scale;
     warm.energy_level = int(kSeedLevel);
@@ -90,11 +122,26 @@ int learned_enqueue(pdflow_solver* s, cudaStream_t st, unsigned pairs, const voi
     return PDFLOW_OK;
 }
 
-int slots_plain(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void*)
+struct TailCtx {
+    float iter_scale;
+    bool restore;            // put the kept plain 60x80 solution back first
+    const unsigned* map;
+};
+
+// The levels finer than 60x80 for the mapped pairs, from the 60x80 solution in sol.
+int learned_tail(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void* vctx)
 {
-    SolvePlan plan;
-    plan.map = s->map;
-    return enqueue_solve(s, st, pairs, plan);
+    const TailCtx& c = *static_cast<const TailCtx*>(vctx);
+    if (c.restore)
+        if (cudaError_t e = launch_sol_keep(s, pairs, c.map, false, st))
+            return set_error_code(PDFLOW_ERR_CUDA, "restore the plain 60x80 solution", e);
+    SolvePlan tail;
+    tail.first = kSeedLevel + 1;
+    tail.iter_scale = c.iter_scale;
+    tail.map = c.map;
+    const int rc = enqueue_solve(s, st, pairs, tail);
+    if (rc == PDFLOW_OK && c.restore) s->launches += 1;
+    return rc;
 }
 
 unsigned scale_kind(float scale, bool mapped)
@@ -103,6 +150,15 @@ unsigned scale_kind(float scale, bool mapped)
     std::memcpy(&b, &scale, 4);
     return 0x10000000u ^ (b >> 4) ^ (mapped ? 0x20000000u : 0u);
 }
+
+// graph kinds of the two continuations (the head's kinds have bit 28 set)
+unsigned tail_kind(float scale)
+{
+    uint32_t b;
+    std::memcpy(&b, &scale, 4);
+    return 0x40000000u ^ (b >> 4);
+}
+constexpr unsigned kKindFallbackTail = 2u;
 
 int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_net* net,
                   const pdflow_learned_opts* opts, pdflow_learned_report* report)
@@ -162,9 +218,21 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
         for (unsigned k = 0; k < n; ++k) ids[k] = k;
     }
 
+    if (!s->sol_keep) {   // outside any capture: the graphs below only use it
+        void* p = nullptr;
+        const size_t keep = sizeof(float) * 10 * kSeedN * s->batch;
+        if (cudaMalloc(&p, keep + sizeof(unsigned) * s->batch) != cudaSuccess) {
+            cudaGetLastError();
+            set_last_error("learned-path buffers");
+            return PDFLOW_ERR_OOM;
+        }
+        s->sol_keep = static_cast<float*>(p);
+        s->map2 = reinterpret_cast<unsigned*>(static_cast<char*>(p) + keep);
+    }
     LearnedCtx ctx{net, o.iter_scale, slots != nullptr};
     int rc = run_graphed(s, n, scale_kind(o.iter_scale, slots != nullptr), learned_enqueue, &ctx, net);
     if (rc) return rc;
+    unsigned launches = s->launches;
     std::vector<float> e(2 * size_t(s->batch));
     cudaError_t ce = cudaMemcpyAsync(e.data(), s->energy, sizeof(float) * 2 * s->batch, cudaMemcpyDeviceToHost,
                                      s->stream);
@@ -172,22 +240,34 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
     rc = check_status(s);
     if (rc) return rc;
 
-    std::vector<unsigned> fall;
+    std::vector<unsigned> fall, keep;
     float worst = 0.f;
     for (unsigned k = 0; k < n; ++k) {
         const float ep = e[k], el = e[s->batch + k];
         const float ratio = ep > 0.f ? el / ep : (el > 0.f ? INFINITY : 1.f);
         if (!(ratio <= worst)) worst = ratio;   // NaN propagates as "worst"
         if (o.energy_margin >= 0.f && !(el <= (1.f + o.energy_margin) * ep)) fall.push_back(ids[k]);
+        else keep.push_back(ids[k]);
+    }
+    // the head graph has finished (its energies were read), so both maps are free
+    if (!keep.empty()) {
+        ce = cudaMemcpyAsync(s->map, keep.data(), sizeof(unsigned) * keep.size(), cudaMemcpyHostToDevice, s->stream);
+        if (ce != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "H2D accepted slots", ce);
+        const TailCtx tc{o.iter_scale, false, s->map};
+        rc = run_graphed(s, unsigned(keep.size()), tail_kind(o.iter_scale), learned_tail, &tc);
+        if (rc) return rc;
+        launches += s->launches;
     }
     if (!fall.empty()) {
-        ce = cudaMemcpyAsync(s->map, fall.data(), sizeof(unsigned) * fall.size(), cudaMemcpyHostToDevice, s->stream);
+        ce = cudaMemcpyAsync(s->map2, fall.data(), sizeof(unsigned) * fall.size(), cudaMemcpyHostToDevice,
+                             s->stream);
         if (ce != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "H2D fallback slots", ce);
-        const unsigned launches = s->launches;
-        rc = run_graphed(s, unsigned(fall.size()), 1u, slots_plain, nullptr);
-        s->launches += launches;
+        const TailCtx tc{1.f, true, s->map2};
+        rc = run_graphed(s, unsigned(fall.size()), kKindFallbackTail, learned_tail, &tc);
         if (rc) return rc;
+        launches += s->launches;
     }
+    s->launches = launches;   // the continuations run asynchronously, as a plain solve does
     if (report) {
         report->fallbacks = unsigned(fall.size());
         report->max_energy_ratio = worst;

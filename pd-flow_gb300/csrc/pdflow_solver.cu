@@ -511,6 +511,7 @@ int pdflow_destroy(pdflow_solver* s)
     if (s->mixed_graph) cudaGraphExecDestroy(s->mixed_graph);
     if (s->map_table) cudaFree(s->map_table);
     if (s->stage_rgb) cudaFree(s->stage_rgb);
+    if (s->sol_keep) cudaFree(s->sol_keep);
     cudaFree(s->arena);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;

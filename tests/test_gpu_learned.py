@@ -85,3 +85,29 @@ def test_fallback_pairs_equal_the_plain_solve(vga_batch):
     for k in np.nonzero(fell)[0]:
         for c in range(3):
             assert np.array_equal(out[c][k].view(np.uint32), d["plain"][c][k].view(np.uint32))
+
+
+def test_accepted_and_rejected_pairs_in_one_batch(vga_batch):
+    """With a margin that splits the batch, the accepted pairs equal the same
+    learned solve without a fallback rule and the rejected ones equal the
+    plain solve, bit for bit."""
+    d = vga_batch
+    net = Net(PAIRS)
+    net.set_params(load_weights())
+    for scale in (0.5, 0.25, 0.1):   # fewer iterations raise the learned energies
+        d["b"].solve_learned(PAIRS, net, iter_scale=scale, energy_margin=-1.0)
+        free = d["b"].read_flow(PAIRS)
+        ep, el = d["b"].learned_energies(PAIRS)
+        ratio = el / ep
+        if ratio.max() > 1.0 and ratio.min() < ratio.max():
+            break
+    margin = float((ratio.max() + max(1.0, ratio.min())) / 2) - 1.0
+    rep = d["b"].solve_learned(PAIRS, net, iter_scale=scale, energy_margin=margin)
+    out = d["b"].read_flow(PAIRS)
+    net.close()
+    fell = ~(el <= np.float32(1.0 + np.float32(margin)) * ep)
+    assert 0 < rep["fallbacks"] == int(fell.sum()) < PAIRS
+    for k in range(PAIRS):
+        ref = d["plain"] if fell[k] else free
+        for c in range(3):
+            assert np.array_equal(out[c][k].view(np.uint32), ref[c][k].view(np.uint32)), (k, c, bool(fell[k]))
