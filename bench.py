@@ -253,18 +253,27 @@ def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
                 ih, zh = ii.cpu().numpy(), zz.cpu().numpy().view(np.uint16)
                 frames += [(ih[q], zh[q]) for q in range(len(ks))]
             streams.append((sc.width, sc.height, frames))
-    srv = Server(device_budget_bytes=64 << 30, slots_per_lane=4, learned=True, iter_scale=iter_scale,
-                 energy_margin=margin, net_params=weights)
-    infos, _, summary = simulate(srv, streams, rate_hz=rate, seed=1)
-    vga_lat = [i["done_ms"] - i["submit_ms"] for i in infos if i["has_flow"] and streams[i["stream_id"]][1] == 480]
-    qvga_lat = [i["done_ms"] - i["submit_ms"] for i in infos if i["has_flow"] and streams[i["stream_id"]][1] == 240]
-    st = srv.stats()
-    srv.close()
-    summary.update(vga_p50_ms=float(np.percentile(vga_lat, 50)), vga_p99_ms=float(np.percentile(vga_lat, 99)),
-                   qvga_p50_ms=float(np.percentile(qvga_lat, 50)), qvga_p99_ms=float(np.percentile(qvga_lat, 99)),
-                   lanes=st["lanes"], batches=st["batches"], device_bytes=st["device_bytes"],
-                   streams_desc="8 QVGA rows=240 + 8 VGA rows=480, Poisson arrivals at 30 Hz each, "
-                                f"{seconds:.0f} s of frames")
+    def run(learned, streams_used):
+        srv = Server(device_budget_bytes=64 << 30, slots_per_lane=2, learned=learned,
+                     iter_scale=iter_scale if learned else 1.0, energy_margin=margin,
+                     net_params=weights if learned else None)
+        infos, _, summary = simulate(srv, streams_used, rate_hz=rate, seed=1)
+        lat = {r: [i["done_ms"] - i["submit_ms"] for i in infos
+                   if i["has_flow"] and streams_used[i["stream_id"]][1] == r] for r in (240, 480)}
+        st = srv.stats()
+        srv.close()
+        summary.update(vga_p50_ms=float(np.percentile(lat[480], 50)), vga_p99_ms=float(np.percentile(lat[480], 99)),
+                       qvga_p50_ms=float(np.percentile(lat[240], 50)), qvga_p99_ms=float(np.percentile(lat[240], 99)),
+                       lanes=st["lanes"], batches=st["batches"], device_bytes=st["device_bytes"])
+        return summary
+
+    summary = run(True, streams)
+    summary["streams_desc"] = ("8 QVGA rows=240 + 8 VGA rows=480, Poisson arrivals at 30 Hz each, "
+                               f"{seconds:.0f} s of frames, 2 streams per lane")
+    # the same request loop with the plain schedule (first half of the frames), for comparison
+    half = [(w, h, fr[:max(2, len(fr) // 2)]) for w, h, fr in streams]
+    plain = run(False, half)
+    summary["plain_schedule"] = {k: plain[k] for k in ("p50_ms", "p99_ms", "vga_p50_ms", "vga_p99_ms", "flows")}
     return summary
 
 

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/pdflow.h"
+#include "../../include/pdflow_net.h"
 #include "pdflow_iterate.cuh"
 #include "pdflow_kernels.cuh"
 
@@ -102,6 +103,10 @@ using EnqueueFn = int (*)(pdflow_solver* s, cudaStream_t st, unsigned pairs, con
 int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx,
                 const void* key = nullptr);
 int set_error_code(int code, const char* what, cudaError_t e = cudaSuccess);
+// The learned slot solve with every pair sent down the fallback path (the
+// serving lanes' graph warm-up uses it to capture the fallback graphs).
+int learned_solve_all_fallback(pdflow_solver* s, unsigned n, const unsigned* slots, ::pdflow_net* net,
+                               const ::pdflow_learned_opts* opts);
 int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);
 int check_status(pdflow_solver* s);
 void set_last_error(const char* text);   // the text pdflow_last_error returns on this thread

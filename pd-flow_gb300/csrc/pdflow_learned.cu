@@ -161,7 +161,7 @@ unsigned tail_kind(float scale)
 constexpr unsigned kKindFallbackTail = 2u;
 
 int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_net* net,
-                  const pdflow_learned_opts* opts, pdflow_learned_report* report)
+                  const pdflow_learned_opts* opts, pdflow_learned_report* report, bool force_fallback = false)
 {
     if (!s || !net) {
         set_last_error("null argument");
@@ -246,7 +246,8 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
         const float ep = e[k], el = e[s->batch + k];
         const float ratio = ep > 0.f ? el / ep : (el > 0.f ? INFINITY : 1.f);
         if (!(ratio <= worst)) worst = ratio;   // NaN propagates as "worst"
-        if (o.energy_margin >= 0.f && !(el <= (1.f + o.energy_margin) * ep)) fall.push_back(ids[k]);
+        if (force_fallback || (o.energy_margin >= 0.f && !(el <= (1.f + o.energy_margin) * ep)))
+            fall.push_back(ids[k]);
         else keep.push_back(ids[k]);
     }
     // the head graph has finished (its energies were read), so both maps are free
@@ -276,6 +277,12 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
 }
 
 }  // namespace
+
+int pdflow::learned_solve_all_fallback(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_net* net,
+                                       const pdflow_learned_opts* opts)
+{
+    return learned_solve(s, n, slots, net, opts, nullptr, true);
+}
 
 extern "C" {
 

@@ -242,8 +242,11 @@ int add_lane(pdflow_server* srv, unsigned width, unsigned height, Lane** out)
             } else {
                 rc = pdflow_solve_slots(L->solver, n, slots.data());
             }
-            // the plain slot solve is also the fallback path of the learned one
-            if (!rc && srv->cfg.learned) rc = pdflow_solve_slots(L->solver, n, slots.data());
+            // and the learned solve's fallback continuation for n pairs
+            if (!rc && srv->cfg.learned) {
+                pdflow_learned_opts o{srv->cfg.iter_scale, srv->cfg.energy_margin};
+                rc = pdflow::learned_solve_all_fallback(L->solver, n, slots.data(), L->net, &o);
+            }
         }
         if (!rc) rc = pdflow_synchronize(L->solver);
         if (rc) {
