@@ -3,12 +3,14 @@
 //   C[M, N] (+)= A[M, K] * B[N, K]^T        A, B: bf16, K contiguous
 //
 // One CTA of 128 threads owns a 128 x BN tile of C (BN = 16..128, multiple of
-// 16).  K advances in chunks of 64: all threads stage the A and B chunks in
-// shared memory in the canonical no-swizzle K-major layout (8-row x 16-byte
-// core matrices; 128 B between core matrices along K, 1024 B between 8-row
-// groups), one elected thread issues four tcgen05.mma (K = 16 each) into an
-// FP32 accumulator in tensor memory and commits them to the stage's mbarrier,
-// which frees the stage two chunks later (double buffering).  The epilogue
+// 16).  K advances in chunks of 64 through a 3-stage ring: all threads copy
+// the A and B chunks into shared memory with asynchronous 16-byte copies
+// (cp.async, two chunks ahead of the one being multiplied) in the canonical
+// no-swizzle K-major layout (8-row x 16-byte core matrices; 128 B between core
+// matrices along K, 1024 B between 8-row groups), one elected thread issues
+// four tcgen05.mma (K = 16 each) into an FP32 accumulator in tensor memory and
+// commits them to the stage's mbarrier, which frees the stage for the chunk
+// three ahead.  The epilogue
 // reads the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 =
 // rows of the tile), adds the bias, applies ReLU and stores FP32 or BF16.
 // grid.z splits K (split-K partials go to C + z * split_stride).
@@ -28,7 +30,8 @@ constexpr int kBM = 128, kBK = 64, kMaxBN = 128, kThreads = 128;
 constexpr uint32_t kTmemCols = 128;
 constexpr int kStageA = kBM * kBK * 2;         // 16 KB
 constexpr int kStageB = kMaxBN * kBK * 2;      // 16 KB
-constexpr int kSmemBytes = 2 * (kStageA + kStageB) + 64;
+constexpr int kStages = 3;
+constexpr int kSmemBytes = kStages * (kStageA + kStageB) + 64;
 constexpr uint32_t kWaitLimit = 1u << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -74,28 +77,35 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity)
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// Stages rows [row0, row0 + rows) x K chunk [k0, k0 + 64) of a K-major bf16
-// matrix into the core-matrix layout; rows >= nrows and k >= K read as zero.
+// Starts the asynchronous copy of rows [row0, row0 + rows) x K chunk
+// [k0, k0 + 64) of a K-major bf16 matrix into the core-matrix layout; rows >=
+// nrows and k >= K are zero-filled (source size 0, the source address is then
+// the matrix base and nothing is read).  K is a multiple of 8, so a 16-byte
+// piece is wholly inside or wholly outside.
 __device__ __forceinline__ void stage_tile(unsigned char* dst, const __nv_bfloat16* src, int ld, int row0,
                                            int rows, int nrows, int k0, int K)
 {
-    const int chunks = rows * 8;   // 16-byte chunks
+    const int chunks = rows * 8;   // 16-byte pieces
     for (int c = threadIdx.x; c < chunks; c += kThreads) {
         const int r = c % rows, kc = c / rows;
         const int gr = row0 + r, gk = k0 + kc * 8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gr < nrows && gk < K) v = *reinterpret_cast<const uint4*>(src + (size_t)gr * ld + gk);
-        *reinterpret_cast<uint4*>(dst + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16) = v;
+        const bool in = gr < nrows && gk < K;
+        const __nv_bfloat16* g = in ? src + (size_t)gr * ld + gk : src;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                         smem_u32(dst + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16)),
+                     "l"(g), "r"(in ? 16 : 0)
+                     : "memory");
     }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sA[2] = {smem, smem + kStageA};
-    unsigned char* sB[2] = {smem + 2 * kStageA, smem + 2 * kStageA + kStageB};
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 2 * (kStageA + kStageB));
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
+    // stage i: A at smem + i * kStageA, B after all A stages
+    auto sA = [&](int i) { return smem + i * kStageA; };
+    auto sB = [&](int i) { return smem + kStages * kStageA + i * kStageB; };
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kStages * (kStageA + kStageB));
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + kStages);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * a.bn;
     const int kbeg = blockIdx.z * a.k_per_split;
@@ -103,8 +113,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
     const int nk = kend > kbeg ? (kend - kbeg + kBK - 1) / kBK : 0;
 
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])));
+#pragma unroll
+        for (int i = 0; i < kStages; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[i])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -119,16 +130,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
     const uint32_t idesc = instr_desc(a.bn);
     bool ok = true;
 
+    const __nv_bfloat16* A = static_cast<const __nv_bfloat16*>(a.A);
+    const __nv_bfloat16* B = static_cast<const __nv_bfloat16*>(a.B);
+    // prologue: chunks 0 .. kStages-2, one commit group each (empty past the end)
+#pragma unroll
+    for (int i = 0; i < kStages - 1; ++i) {
+        if (i < nk) {
+            stage_tile(sA(i), A, a.lda, m0, kBM, a.M, kbeg + i * kBK, kend);
+            stage_tile(sB(i), B, a.ldb, n0, a.bn, a.N, kbeg + i * kBK, kend);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     for (int kc = 0; kc < nk; ++kc) {
-        const int s = kc & 1;
-        if (kc >= 2) ok &= mbar_wait(smem_u32(&mbar[s]), uint32_t(((kc - 2) >> 1) & 1));
-        stage_tile(sA[s], static_cast<const __nv_bfloat16*>(a.A), a.lda, m0, kBM, a.M, kbeg + kc * kBK, kend);
-        stage_tile(sB[s], static_cast<const __nv_bfloat16*>(a.B), a.ldb, n0, a.bn, a.N, kbeg + kc * kBK, kend);
+        const int s = kc % kStages;
+        // groups committed so far: kStages - 1 + kc; chunk kc's is complete when
+        // at most kStages - 2 younger ones are pending
+        asm volatile("cp.async.wait_group %0;" ::"n"(kStages - 2) : "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
             fence_after();
-            const uint32_t abase = smem_u32(sA[s]), bbase = smem_u32(sB[s]);
+            const uint32_t abase = smem_u32(sA(s)), bbase = smem_u32(sB(s));
 #pragma unroll
             for (int ks = 0; ks < kBK / 16; ++ks) {
                 const uint64_t ad = smem_desc(abase + ks * 256, 128, 1024);
@@ -144,8 +166,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
                              smem_u32(&mbar[s]))
                          : "memory");
         }
+        // refill: chunk kc + kStages - 1 goes into the stage chunk kc - 1 used,
+        // once that chunk's multiplies have completed
+        const int nc = kc + kStages - 1;
+        if (nc < nk) {
+            const int ns = nc % kStages;
+            if (kc >= 1) ok &= mbar_wait(smem_u32(&mbar[ns]), uint32_t(((kc - 1) / kStages) & 1));
+            stage_tile(sA(ns), A, a.lda, m0, kBM, a.M, kbeg + nc * kBK, kend);
+            stage_tile(sB(ns), B, a.ldb, n0, a.bn, a.N, kbeg + nc * kBK, kend);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    if (nk > 0) ok &= mbar_wait(smem_u32(&mbar[(nk - 1) & 1]), uint32_t(((nk - 1) >> 1) & 1));
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (nk > 0) ok &= mbar_wait(smem_u32(&mbar[(nk - 1) % kStages]), uint32_t(((nk - 1) / kStages) & 1));
     fence_after();
 
     // ---- epilogue: warp w holds rows 32w..32w+31 of the tile ----

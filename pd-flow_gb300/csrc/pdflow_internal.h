@@ -26,6 +26,7 @@ struct pdflow_solver {
     uint8_t* stage_u8 = nullptr;         // device staging of a raw frame
     uint16_t* stage_u16 = nullptr;
     uint8_t* stage_rgb = nullptr;        // device staging of RGB888 frames (allocated on first use)
+    double* energy_part = nullptr;       // energy partial sums [batch][1024]
     float* sol_keep = nullptr;           // learned path: the plain 60x80 solutions [slot][10][4800] and ...
     unsigned* map2 = nullptr;            // ... a second slot map [batch] (one allocation, on first use)
     pdflow::LevelConsts L{};

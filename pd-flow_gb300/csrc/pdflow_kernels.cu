@@ -621,18 +621,24 @@ __global__ void k_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L)
     at(L.dv_prev, po)[i] = at(sol.dv, po)[i];
 }
 
-// One CTA per pair; fixed thread-to-pixel assignment and a fixed reduction
-// tree, so the sum is deterministic.  With du = dv = 0 increments at the warp
-// point the linearised data terms equal the warped residuals.
-__global__ void __launch_bounds__(1024) k_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p,
-                                                 float* __restrict__ energies)
+// 1024 accumulators per pair: accumulator t sums pixels t, t + 1024, ... in
+// that order (32 one-warp CTAs per pair, so the FP64 work of one pair spreads
+// over 32 SMs); k_energy_sum then adds the 1024 partial sums of a pair in a
+// fixed tree, so the energy is deterministic and independent of the batch.
+// With du = dv = 0 increments at the warp point the linearised data terms
+// equal the warped residuals.
+constexpr unsigned kEnergyAcc = 1024;
+
+__global__ void __launch_bounds__(32) k_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p,
+                                               double* __restrict__ part)
 {
     const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     sol = at(sol, po);
     L = at(L, po);
     const unsigned R = g.R, C = g.C;
+    const unsigned t = blockIdx.x * 32 + threadIdx.x;
     double acc = 0.0;
-    for (unsigned i = threadIdx.x; i < g.N; i += blockDim.x) {
+    for (unsigned i = t; i < g.N; i += kEnergyAcc) {
         const unsigned v = i % R, u = i / R;
         const float U = sol.du[i], V = sol.dv[i], W = sol.dw[i], ri = L.ri[i], rj = L.rj[i];
         const bool lu = u == C - 1, lv = v == R - 1;
@@ -644,8 +650,14 @@ __global__ void __launch_bounds__(1024) k_energy(LevelGeom g, LevelSol sol, Leve
         e += (double)p.lambda_d * hypot((double)gw1, (double)gw2);
         acc += e;
     }
-    __shared__ double red[1024];
-    red[threadIdx.x] = acc;
+    part[(size_t)blockIdx.y * kEnergyAcc + t] = acc;
+}
+
+__global__ void __launch_bounds__(kEnergyAcc) k_energy_sum(const double* __restrict__ part,
+                                                           float* __restrict__ energies)
+{
+    __shared__ double red[kEnergyAcc];
+    red[threadIdx.x] = part[(size_t)blockIdx.y * kEnergyAcc + threadIdx.x];
     __syncthreads();
     for (unsigned w = blockDim.x / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
@@ -749,9 +761,13 @@ cudaError_t launch_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, cudaStream_t st)
+cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, double* part,
+                          cudaStream_t st)
 {
-    k_energy<<<dim3(1, g.pairs), 1024, 0, st>>>(g, sol, L, p, energies);
+    k_energy<<<dim3(kEnergyAcc / 32, g.pairs), 32, 0, st>>>(g, sol, L, p, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_energy_sum<<<dim3(1, g.pairs), kEnergyAcc, 0, st>>>(part, energies);
     return cudaGetLastError();
 }
 

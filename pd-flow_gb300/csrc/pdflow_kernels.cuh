@@ -127,7 +127,9 @@ cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel
 // sum over pixels of |dct| + mu |ddt - dw| + lambda_i (|r grad du| + |r grad dv|)
 // + lambda_d |r grad dw|; energies[y] for grid index y.
 cudaError_t launch_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L, cudaStream_t st);
-cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, cudaStream_t st);
+// part: device scratch of 1024 doubles per pair.
+cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, double* part,
+                          cudaStream_t st);
 cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st);
 cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p,
                               cudaStream_t st);

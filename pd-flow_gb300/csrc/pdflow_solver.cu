@@ -138,6 +138,7 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     s->status = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * 4));
     s->map = static_cast<unsigned*>(cv.bytes(sizeof(unsigned) * s->batch));
     s->energy = static_cast<float*>(cv.bytes(sizeof(float) * 2 * s->batch));
+    s->energy_part = static_cast<double*>(cv.bytes(sizeof(double) * 1024 * s->batch));
     s->seed = (s->ctf_levels > kSeedLevel) || s->rows == 60 ? cv.plane(size_t(3) * kSeedN * s->batch) : nullptr;
     *used = cv.off;
 }
@@ -288,8 +289,8 @@ int enqueue_energy(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned l
     CUDA_TRY(launch_energy_prep(g, s->sol, s->L, st), "energy prep launch");
     CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
     CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
-    CUDA_TRY(launch_energy(g, s->sol, s->L, p, out, st), "energy launch");
-    s->launches += 4;
+    CUDA_TRY(launch_energy(g, s->sol, s->L, p, out, s->energy_part, st), "energy launch");
+    s->launches += 5;
     return PDFLOW_OK;
 }
 
