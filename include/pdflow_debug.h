@@ -26,11 +26,11 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
 /* Selects how pdflow_solve runs a level's iterations: 5 (default) = every
  * level of a batch (more than one pair), and a single pair's levels above
- * 19 200 pixels, as temporally blocked shared-memory tiles (several
+ * 300 pixels (all but 15x20), as temporally blocked shared-memory tiles (several
  * iterations per launch; 24x24 tiles, one pixel pair per thread in packed
  * FP32x2 arithmetic, two CTAs per SM so that one CTA's region load and store
- * overlap the other's iterations), a single pair's smaller levels as one
- * launch per level; 6 = the same with 24x28 tiles (288 threads owning two
+ * overlap the other's iterations), a single pair's 15x20 level as one
+ * launch; 6 = the same with 24x28 tiles (288 threads owning two
  * pairs each, two CTAs per SM); 4 = the same with 40x34 tiles (1008 threads,
  * one CTA per SM); 3 = the same with 40x40 tiles and two pairs per thread; 2 = one pixel
  * per lane; 1 = one launch per level (slab-persistent kernel; batches use two

@@ -198,10 +198,10 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
         one_launch = forced == 1 && iters > 0 && one_launch_ok;
     } else {
         // batches: tiles at every level (measured faster than the cluster-persistent form
-        // from 15x20 up to 120x160 too); a single pair: tiles for the levels that would
-        // need the whole grid (240x320, 480x640: 11 % faster per VGA solve), the
-        // one-CTA / cluster persistent launch below
-        tiles = s->iter_form >= 2 && iters > 0 && (pairs > 1 || pl.mode == kIterGrid);
+        // from 15x20 up to 120x160 too); a single pair: tiles above 15x20 (per iteration
+        // at 30x40 .. 120x160 about half the time of the one-launch form; whole VGA solves
+        // 2.00 against 2.34 ms, QVGA 1.22 against 1.55 ms), the one-CTA launch at 15x20
+        tiles = s->iter_form >= 2 && iters > 0 && (pairs > 1 || g.N > 300u);
         one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
     }
     const bool paired = tiles && form >= 3;
