@@ -239,7 +239,7 @@ def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
     T = int(seconds * rate)
     streams = []
     for vga in (False, True):
-        scs = [scenes.make_scene(8_000_000 + 100 * vga + j, vga, 3 + j % 4) for j in range(8)]
+        scs = [scenes.make_scene(8_000_000 + 100 * vga + j, vga, 3 + j % 4, period=10) for j in range(8)]
         for j, sc in enumerate(scs):
             frames = []
             for k0 in range(0, T, 30):

@@ -14,7 +14,9 @@ moving rigidly by at most 5 cm and 3 degrees between the two frames.
 
 Images are row-major (height, width), as a PNG decoder returns them.
 Streams (for the serving loop) keep each object's per-frame rigid motion, so
-frame k is the scene after k steps of a constant-velocity trajectory.
+frame k is the scene after k steps of a constant-velocity trajectory, or, with
+`period`, of a trajectory that reverses every `period` frames and so stays in
+view for any number of frames.
 """
 from __future__ import annotations
 
@@ -79,10 +81,15 @@ class _Object:
     d_center: np.ndarray    # per-frame translation
     d_rot: np.ndarray       # per-frame rotation (about the object's centre)
     albedo: float
+    period: int = 0         # > 0: the motion reverses every `period` frames (bounded trajectory)
 
     def pose(self, k: int):
+        steps = k
+        if self.period > 0:   # triangle wave: forward `period` frames, back `period` frames
+            m = k % (2 * self.period)
+            steps = m if m <= self.period else 2 * self.period - m
         c, r = self.center.copy(), self.rot.copy()
-        for _ in range(k):
+        for _ in range(steps):
             c = c + self.d_center
             r = self.d_rot @ r
         return c, r
@@ -105,9 +112,11 @@ class Scene:
         return self.cam["height"]
 
 
-def make_scene(seed: int, vga: bool = False, n_objects: int | None = None) -> Scene:
+def make_scene(seed: int, vga: bool = False, n_objects: int | None = None, period: int = 0) -> Scene:
     """Scene for `seed`: plane at 2-4 m plus `n_objects` boxes/spheres at 0.8-2.5 m
-    (default 6 at VGA, 3 at QVGA), each with a rigid motion of <= 5 cm and <= 3 deg."""
+    (default 6 at VGA, 3 at QVGA), each with a rigid motion of <= 5 cm and <= 3 deg
+    per frame.  period > 0 makes long sequences stay in view: each object moves
+    forward for `period` frames, then back (frames 0 and 1 do not depend on it)."""
     rng = np.random.default_rng(seed)
     cam = dict(VGA if vga else QVGA)
     if n_objects is None:
@@ -137,7 +146,7 @@ def make_scene(seed: int, vga: bool = False, n_objects: int | None = None) -> Sc
         d_center = tdir / np.linalg.norm(tdir) * rng.uniform(0.01, 0.05)
         d_rot = _rotation(rng.normal(size=3), math.radians(rng.uniform(0.5, 3.0)))
         objs.append(_Object(kind, np.array([xc, yc, zc]), rot, size, _Noise3(rng, rng.uniform(0.015, 0.04)),
-                            d_center, d_rot, rng.uniform(0.6, 1.0)))
+                            d_center, d_rot, rng.uniform(0.6, 1.0), period))
     return Scene(cam, (z0, a, b), plane_tex, objs, int(rng.integers(1 << 31)))
 
 
