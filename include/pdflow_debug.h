@@ -78,6 +78,16 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
  * plain loads and stores.  All modes give the same bits. */
 int pdflow_set_tile_copy_mode(int shape, int mode);
 
+/* Failure detection without a fault: on the handle's stream, two CTAs where
+ * one waits, through the bounded neighbour wait of the one-launch grid form
+ * limited to `polls` polls (1..1e7), for a progress counter the other never
+ * sets.  The wait runs out, the kernel records a timeout in the handle's
+ * status word and returns; this call then reports it the way every
+ * synchronising call does (PDFLOW_ERR_TIMEOUT, the status word reset) and
+ * the handle stays usable.  No counterpart in the reference, which checks no
+ * errors. */
+int pdflow_debug_wait_timeout(pdflow_solver* s, unsigned polls);
+
 #ifdef __cplusplus
 }
 #endif

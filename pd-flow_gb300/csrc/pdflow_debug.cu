@@ -222,6 +222,14 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
     return pdflow::check_status(s);
 }
 
+int pdflow_debug_wait_timeout(pdflow_solver* s, unsigned polls)
+{
+    if (!s || polls == 0 || polls > 10000000u) return fail(PDFLOW_ERR_ARG, "polls 1..1e7");
+    const cudaError_t e = launch_wait_probe(s->flags, s->status, polls, s->stream);
+    if (e != cudaSuccess) return fail("wait probe launch", e);
+    return pdflow::check_status(s);
+}
+
 int pdflow_set_tile_copy_mode(int shape, int mode)
 {
     if (shape < 0 || shape > 3 || mode < 0 || mode > 3) return fail(PDFLOW_ERR_ARG, "shape 0..3, mode 0..3");

@@ -48,8 +48,9 @@ __device__ __forceinline__ void st_release(unsigned* p, unsigned v)
 }
 
 // Thread 0 waits until both neighbouring slabs have completed `need`
-// iterations.  Returns false (after recording the failure) on timeout.
-__device__ bool wait_neighbours(const IterArgs& a, unsigned need)
+// iterations, polling at most `limit` times.  Returns false (after recording
+// the failure) on timeout.
+__device__ bool wait_neighbours(const IterArgs& a, unsigned need, unsigned long long limit = kSpinLimit)
 {
     __shared__ int ok;
     if (threadIdx.x == 0) {
@@ -58,11 +59,11 @@ __device__ bool wait_neighbours(const IterArgs& a, unsigned need)
         unsigned long long spins = 0;
         if (b > 0)
             while (ld_acquire(a.flags + b - 1) < need) {
-                if (++spins > kSpinLimit || ld_acquire(a.status) != 0) { ok = 0; break; }
+                if (++spins > limit || ld_acquire(a.status) != 0) { ok = 0; break; }
             }
         if (ok && b + 1 < gridDim.x)
             while (ld_acquire(a.flags + b + 1) < need) {
-                if (++spins > kSpinLimit || ld_acquire(a.status) != 0) { ok = 0; break; }
+                if (++spins > limit || ld_acquire(a.status) != 0) { ok = 0; break; }
             }
         if (!ok) atomicCAS(a.status, 0u, kStatusTimeout);
     }
@@ -249,6 +250,16 @@ __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
     }
 }
 
+// Failure-detection probe: CTA 1 waits, through wait_neighbours with `limit`
+// polls, for CTA 0 to complete an iteration, and CTA 0 never publishes one
+// (its counter is a flag nothing sets), so the wait runs out and records
+// kStatusTimeout; both CTAs return.
+__global__ void k_wait_probe(IterArgs a, unsigned limit)
+{
+    if (blockIdx.x == 0) return;
+    wait_neighbours(a, 1u, limit);
+}
+
 unsigned g_max_cluster = 8;    // largest cluster the GPU places with this kernel's resources
 unsigned g_max_dyn_smem = 0;   // dynamic shared memory available to the iteration kernels
 
@@ -324,6 +335,17 @@ cudaError_t prepare_iterate()
     else
         cudaGetLastError();
     return cudaSuccess;
+}
+
+cudaError_t launch_wait_probe(unsigned* flags, unsigned* status, unsigned polls, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    IterArgs a{};
+    a.flags = flags;
+    a.status = status;
+    k_wait_probe<<<2, 32, 0, st>>>(a, polls);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st)

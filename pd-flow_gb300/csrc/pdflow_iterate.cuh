@@ -56,6 +56,10 @@ cudaError_t prepare_tiles2();
 cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
                                   unsigned kk, bool last, cudaStream_t st, int shape = 0,
                                   unsigned* status = nullptr);
+// Failure-detection probe: two CTAs where one waits (the grid form's bounded
+// neighbour wait, `polls` polls) for a progress counter the other never sets;
+// the wait runs out and records kStatusTimeout in *status.  flags: 2 counters.
+cudaError_t launch_wait_probe(unsigned* flags, unsigned* status, unsigned polls, cudaStream_t st);
 // Enqueues the level's iterations (and, in the grid form, the reset of the progress counters).
 cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st);
 

@@ -178,6 +178,7 @@ _SIGNATURES = {
     "pdflow_autotune": (ctypes.c_int, [vp, u32, u32, ctypes.POINTER(TuneReport)]),
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "pdflow_debug_wait_timeout": (ctypes.c_int, [vp, u32]),
     "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),
     "pdflow_push_frames_mixed": (ctypes.c_int, [vp, u32, vp, vp, vp, vp, vp]),
     "pdflow_solve_mixed": (ctypes.c_int, [vp, u32]),

@@ -77,6 +77,7 @@ def test_null_handles_are_rejected(built_lib):
     assert built_lib.pdflow_solve(None) == _lib.ERR_ARG
     assert built_lib.pdflow_read_flow(None, None, None, None) == _lib.ERR_ARG
     assert built_lib.pdflow_destroy(None) == _lib.OK
+    assert built_lib.pdflow_debug_wait_timeout(None, 1000) == _lib.ERR_ARG
 
 
 def test_cpp_host_class_compiles():
