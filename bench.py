@@ -377,6 +377,19 @@ def ours(args):
     torch.cuda.synchronize()
     batched_plain = {"pairs_s": B * max(3, K // 2) / (ta.elapsed_time(tb) / 1000.0), "epe_vs_plain_mm": 0.0}
 
+    # per-level phase times of one eager (ungraphed) plain solve of the batch:
+    # set-up, iterations (with their algorithmic bandwidth) and median per level
+    with torch.cuda.stream(stream):
+        push()
+        tr = b.trace(B)
+    trace = []
+    for i, t in enumerate(tr):
+        Ri, Ci, it = 15 << i, 20 << i, 100 - 15 * (len(tr) - 1 - i)
+        trace.append({"level": f"{Ri}x{Ci}", "iterations": it, "setup_ms": round(t["setup_ms"], 4),
+                      "iterations_ms": round(t["iterations_ms"], 4), "median_ms": round(t["median_ms"], 4),
+                      "iterations_alg_gbs": round(ALG_BYTES_PER_PX_ITER * B * Ri * Ci * it
+                                                  / (t["iterations_ms"] / 1e3) / 1e9, 1)})
+
     # the learned warm start with the finer levels' iterations halved (the
     # schedule's nominal setting), same handle, frames and fallback rule
     half = 0.5
@@ -515,7 +528,8 @@ def ours(args):
             "accuracy": accuracy,
             "batched": {"pairs_s": value, "p50_ms_per_batch": statistics.median(step_ms),
                         "p99_ms_per_batch": float(np.quantile(step_ms, 0.99))},
-            "batched_plain": batched_plain, "learned_half_iterations": learned_half, "mixed_batch": mixed,
+            "batched_plain": batched_plain, "plain_batch_trace": trace, "learned_half_iterations": learned_half,
+            "mixed_batch": mixed,
             "plain": plain,
             "speedup_vs_plain_single": value / plain["pairs_s"],
             "p99_ms": serving["vga_p99_ms"] if serving and "vga_p99_ms" in serving else None,

@@ -78,6 +78,15 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
  * plain loads and stores.  All modes give the same bits. */
 int pdflow_set_tile_copy_mode(int shape, int mode);
 
+/* Per-level, per-phase timing of a plain solve of pairs [0, n) (tracing; no
+ * counterpart in the reference, whose only timing is a host clock around the
+ * whole solve): runs the solve eagerly (no graph) on the handle's stream with
+ * CUDA events before each level's set-up (upsampling, gradients, warping),
+ * iterations and median, and fills ms[3 * level + phase] (phase 0 = set-up,
+ * 1 = iterations, 2 = median and motion field) for every level, coarsest
+ * first (ms has 3 * ctf_levels entries).  The flow is the plain solve's. */
+int pdflow_trace_solve(pdflow_solver* s, unsigned n, float* ms);
+
 /* Failure detection without a fault: on the handle's stream, two CTAs where
  * one waits, through the bounded neighbour wait of the one-launch grid form
  * limited to `polls` polls (1..1e7), for a progress counter the other never

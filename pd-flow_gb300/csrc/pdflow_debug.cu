@@ -172,6 +172,31 @@ int pdflow_time_level_iterations(pdflow_solver* s, unsigned n, unsigned level, u
     return e == cudaSuccess ? PDFLOW_OK : fail("timing", e);
 }
 
+int pdflow_trace_solve(pdflow_solver* s, unsigned n, float* ms)
+{
+    if (!s || !ms || n == 0 || n > s->batch) return fail(PDFLOW_ERR_ARG, "bad pair count or null output");
+    if (s->slot_mode) return fail(PDFLOW_ERR_STATE, "frames were pushed per slot");
+    if (s->frames < 2) return fail(PDFLOW_ERR_STATE, "solve needs two pushed frames");
+    const unsigned L = s->ctf_levels, ne = 3 * L + 1;
+    std::vector<cudaEvent_t> ev(ne, nullptr);
+    cudaError_t e = cudaSuccess;
+    for (unsigned k = 0; k < ne && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+    int rc = PDFLOW_OK;
+    if (e == cudaSuccess) {
+        SolvePlan plan;
+        plan.trace = ev.data();
+        rc = enqueue_solve(s, s->stream, n, plan);
+        if (rc == PDFLOW_OK) e = cudaEventSynchronize(ev[ne - 1]);
+        for (unsigned k = 0; k + 1 < ne && rc == PDFLOW_OK && e == cudaSuccess; ++k)
+            e = cudaEventElapsedTime(ms + k, ev[k], ev[k + 1]);
+    }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    if (rc != PDFLOW_OK) return rc;
+    if (e != cudaSuccess) return fail("trace events", e);
+    return pdflow::check_status(s);
+}
+
 int pdflow_stage_median(unsigned R, unsigned C, const float* depth_old, const float* ddt, const float* du,
                         const float* dv, const float* dw, float* du_l, float* dv_l, float* dw_l, int32_t* sel,
                         void* stream)

@@ -308,11 +308,14 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
         g.map = plan.map;
         const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];
         const float* seed = (i == plan.first) ? plan.seed : nullptr;
+        cudaEvent_t* tr = plan.trace ? plan.trace + 3 * (i - plan.first) : nullptr;
+        if (tr) CUDA_TRY(cudaEventRecord(tr[0], st), "trace event");
         CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st, seed), "level init launch");
         CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
         CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
         count += 3;
         const unsigned iters = scaled_iters(s->prm.num_max_iter[i], plan.iter_scale);
+        if (tr) CUDA_TRY(cudaEventRecord(tr[1], st), "trace event");
         State fin;
         int rc = enqueue_iterations(s, st, g, o, iters, pairs, &fin, &count, i);
         if (rc) return rc;
@@ -320,6 +323,7 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
             CUDA_TRY(launch_saturate(g, s->L, s->S, o.dep, st), "saturate launch");
             ++count;
         }
+        if (tr) CUDA_TRY(cudaEventRecord(tr[2], st), "trace event");
         CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
                  "median launch");
         ++count;
@@ -330,6 +334,7 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
             count += s->launches;
         }
     }
+    if (plan.trace) CUDA_TRY(cudaEventRecord(plan.trace[3 * (last + 1 - plan.first)], st), "trace event");
     s->launches = count;
     return PDFLOW_OK;
 }

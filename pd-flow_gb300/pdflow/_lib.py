@@ -179,6 +179,7 @@ _SIGNATURES = {
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "pdflow_debug_wait_timeout": (ctypes.c_int, [vp, u32]),
+    "pdflow_trace_solve": (ctypes.c_int, [vp, u32, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),
     "pdflow_push_frames_mixed": (ctypes.c_int, [vp, u32, vp, vp, vp, vp, vp]),
     "pdflow_solve_mixed": (ctypes.c_int, [vp, u32]),
@@ -531,6 +532,17 @@ class BatchSolver(_Extras):
         return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
                  "ms_per_iter": [None if not np.isfinite(x) else float(x) for x in rep.level[i].ms_per_iter]}
                 for i in range(rep.levels)]
+
+    def trace(self, n: int):
+        """Per-level phase times of an eager plain solve of pairs [0, n)
+        (pdflow_trace_solve): [{setup_ms, iterations_ms, median_ms}] coarsest first."""
+        rows, cols, ctf = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+        check(load().pdflow_get_config(self._h, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(ctf), None, None),
+              "pdflow_get_config")
+        ms = (ctypes.c_float * (3 * ctf.value))()
+        check(load().pdflow_trace_solve(self._h, n, ms), "pdflow_trace_solve")
+        return [{"setup_ms": ms[3 * i], "iterations_ms": ms[3 * i + 1], "median_ms": ms[3 * i + 2]}
+                for i in range(ctf.value)]
 
     def set_level_form(self, level: int, form: int, iters_per_launch: int = 0):
         check(load().pdflow_set_level_form(self._h, level, form, iters_per_launch), "pdflow_set_level_form")

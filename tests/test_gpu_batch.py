@@ -72,3 +72,23 @@ def test_batch_rejects_bad_counts():
         b.solve(3)
     assert e.value.code == ERR_ARG
     b.close()
+
+
+def test_trace_solve_times_every_phase_and_keeps_the_flow(built_lib):
+    """pdflow_trace_solve: per-level set-up / iterations / median times of an
+    eager solve, whose flow is the plain solve's bit for bit."""
+    pairs = [scenes.make_pair(400 + k) for k in range(2)]
+    b = BatchSolver(240, 320, 240, 2)
+    b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
+    b.push_raw(np.stack([p[2] for p in pairs]), np.stack([p[3] for p in pairs]))
+    b.solve(2)
+    ref = b.read_flow(2)
+    tr = b.trace(2)
+    got = b.read_flow(2)
+    b.close()
+    assert len(tr) == 5
+    for t in tr:
+        assert t["setup_ms"] > 0 and t["iterations_ms"] > 0 and t["median_ms"] > 0
+    assert tr[-1]["iterations_ms"] > tr[0]["iterations_ms"]      # 100 iterations at 240x320 vs 40 at 15x20
+    for x, y in zip(got, ref):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
