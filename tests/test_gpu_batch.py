@@ -92,3 +92,21 @@ def test_trace_solve_times_every_phase_and_keeps_the_flow(built_lib):
     assert tr[-1]["iterations_ms"] > tr[0]["iterations_ms"]      # 100 iterations at 240x320 vs 40 at 15x20
     for x, y in zip(got, ref):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_repeated_solves_are_bit_identical(built_lib):
+    """Determinism: the same frames solved twice (graph replay and an eager
+    stream of kernels) give the same bits."""
+    pairs = [scenes.make_pair(410 + k, vga=True) for k in range(2)]
+    out = []
+    for graph in (True, True, False):
+        b = BatchSolver(480, 640, 480, 2, use_graph=graph)
+        b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
+        b.push_raw(np.stack([p[2] for p in pairs]), np.stack([p[3] for p in pairs]))
+        b.solve(2)
+        b.solve(2)
+        out.append(b.read_flow(2))
+        b.close()
+    for o in out[1:]:
+        for x, y in zip(o, out[0]):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
