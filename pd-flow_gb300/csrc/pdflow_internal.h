@@ -108,6 +108,11 @@ int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, c
 int set_error_code(int code, const char* what, cudaError_t e = cudaSuccess);
 // The learned slot solve with every pair sent down the fallback path (the
 // serving lanes' graph warm-up uses it to capture the fallback graphs).
+// Device bytes of the learned path's buffers (kept 60x80 solutions + second slot map).
+inline size_t learned_keep_bytes(unsigned batch)
+{
+    return (sizeof(float) * 10 * kSeedN + sizeof(unsigned)) * size_t(batch);
+}
 int learned_solve_all_fallback(pdflow_solver* s, unsigned n, const unsigned* slots, ::pdflow_net* net,
                                const ::pdflow_learned_opts* opts);
 int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);

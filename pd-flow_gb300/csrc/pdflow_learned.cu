@@ -221,7 +221,7 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
     if (!s->sol_keep) {   // outside any capture: the graphs below only use it
         void* p = nullptr;
         const size_t keep = sizeof(float) * 10 * kSeedN * s->batch;
-        if (cudaMalloc(&p, keep + sizeof(unsigned) * s->batch) != cudaSuccess) {
+        if (cudaMalloc(&p, learned_keep_bytes(s->batch)) != cudaSuccess) {
             cudaGetLastError();
             set_last_error("learned-path buffers");
             return PDFLOW_ERR_OOM;

@@ -205,6 +205,7 @@ int add_lane(pdflow_server* srv, unsigned width, unsigned height, Lane** out)
     if (rc) return rc;
     L->device_bytes = pdflow_device_bytes(L->solver);
     if (srv->cfg.learned) {
+        L->device_bytes += pdflow::learned_keep_bytes(S);   // allocated by the first learned solve
         rc = pdflow_net_create(S, 1, &L->net);
         if (!rc) rc = pdflow_net_set_params(L->net, srv->params.data(), srv->params.size());
         if (rc) {

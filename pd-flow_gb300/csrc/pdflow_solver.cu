@@ -524,7 +524,14 @@ int pdflow_destroy(pdflow_solver* s)
     return PDFLOW_OK;
 }
 
-size_t pdflow_device_bytes(const pdflow_solver* s) { return s ? s->arena_bytes : 0; }
+size_t pdflow_device_bytes(const pdflow_solver* s)
+{
+    if (!s) return 0;
+    size_t b = s->arena_bytes;   // plus the buffers allocated on first use
+    if (s->sol_keep) b += learned_keep_bytes(s->batch);
+    if (s->stage_rgb) b += size_t(s->width) * s->height * 3 * s->batch;
+    return b;
+}
 
 int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float* Z)
 {
