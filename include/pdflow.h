@@ -105,6 +105,12 @@ int pdflow_read_flow(pdflow_solver* s, float* dx, float* dy, float* dz);
 /* Device pointers of the solver's motion-field planes (valid until destroy). */
 int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, const float** dz);
 
+/* Copies the motion fields of pairs [0, n) into caller device buffers
+ * [n][rows*cols] (column-major per pair) on the solver's stream and returns
+ * without waiting (no counterpart in the reference): a pipeline can then copy
+ * them to the host on another stream while the next batch is solved. */
+int pdflow_copy_flow_device(pdflow_solver* s, unsigned n, float* d_dx, float* d_dy, float* d_dz);
+
 /* Copies pyramid level `level` (0 = full image resolution) of the old
  * (frame = 0) or new (frame = 1) frame: intensity, depth and the
  * back-projected xx, yy, each (height>>level)*(width>>level) floats,

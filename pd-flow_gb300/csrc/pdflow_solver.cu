@@ -657,6 +657,17 @@ int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, con
     return PDFLOW_OK;
 }
 
+int pdflow_copy_flow_device(pdflow_solver* s, unsigned n, float* d_dx, float* d_dy, float* d_dz)
+{
+    if (!s || !d_dx || !d_dy || !d_dz) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
+    const size_t b = size_t(s->rows) * s->cols * 4;
+    CUDA_TRY(cudaMemcpy2DAsync(d_dx, b, s->dx, s->pair_stride, b, n, cudaMemcpyDeviceToDevice, s->stream), "D2D dx");
+    CUDA_TRY(cudaMemcpy2DAsync(d_dy, b, s->dy, s->pair_stride, b, n, cudaMemcpyDeviceToDevice, s->stream), "D2D dy");
+    CUDA_TRY(cudaMemcpy2DAsync(d_dz, b, s->dz, s->pair_stride, b, n, cudaMemcpyDeviceToDevice, s->stream), "D2D dz");
+    return PDFLOW_OK;
+}
+
 int pdflow_batch_info(const pdflow_solver* s, unsigned* max_pairs, size_t* pair_stride_bytes)
 {
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");

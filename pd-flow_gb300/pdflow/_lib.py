@@ -119,6 +119,7 @@ _SIGNATURES = {
     "pdflow_solve": (ctypes.c_int, [vp]),
     "pdflow_read_flow": (ctypes.c_int, [vp, vp, vp, vp]),
     "pdflow_flow_device": (ctypes.c_int, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]),
+    "pdflow_copy_flow_device": (ctypes.c_int, [vp, u32, vp, vp, vp]),
     "pdflow_read_level_images": (ctypes.c_int, [vp, u32, ctypes.c_int, vp, vp, vp, vp]),
     "pdflow_synchronize": (ctypes.c_int, [vp]),
     "pdflow_set_stream": (ctypes.c_int, [vp, vp]),

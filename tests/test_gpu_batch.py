@@ -110,3 +110,23 @@ def test_repeated_solves_are_bit_identical(built_lib):
     for o in out[1:]:
         for x, y in zip(o, out[0]):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_copy_flow_device_matches_read_flow(built_lib):
+    """pdflow_copy_flow_device: all pairs' flows into contiguous device buffers."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from pdflow import _lib
+    pairs = [scenes.make_pair(420 + k) for k in range(3)]
+    b = BatchSolver(120, 320, 240, 4)
+    b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
+    b.push_raw(np.stack([p[2] for p in pairs]), np.stack([p[3] for p in pairs]))
+    b.solve(3)
+    ref = b.read_flow(3)
+    out = torch.zeros((3, 3, 120 * 160), dtype=torch.float32, device="cuda")
+    assert _lib.load().pdflow_copy_flow_device(b.handle, 3, *[ctypes.c_void_p(out[c].data_ptr()) for c in range(3)]) == 0
+    b.synchronize()
+    got = out.cpu().numpy()
+    b.close()
+    for c in range(3):
+        assert np.array_equal(got[c].view(np.uint32), ref[c].view(np.uint32))
