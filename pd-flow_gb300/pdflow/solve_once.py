@@ -23,8 +23,13 @@ def main() -> None:
     ap.add_argument("--learned", type=float, default=0.0,
                     help="iteration scale of a learned warm-started solve (0: plain solve)")
     ap.add_argument("--solves", type=int, default=2)
+    ap.add_argument("--copy-mode", type=int, default=-1, choices=(-1, 0, 1, 2, 3),
+                    help="tile region copies of the chosen paired form (bit 0 bulk load, bit 1 bulk store; -1: default)")
     ap.add_argument("--distinct", type=int, default=4)
     a = ap.parse_args()
+    if a.copy_mode >= 0 and a.form >= 3:
+        from . import _lib
+        _lib.check(_lib.load().pdflow_set_tile_copy_mode(a.form - 3, a.copy_mode), "pdflow_set_tile_copy_mode")
     vga = a.rows == 480
     w, h = (640, 480) if vga else (320, 240)
     pairs = [scenes.make_pair(1000 + k, vga=vga) for k in range(a.distinct)]
