@@ -4,6 +4,8 @@
 
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/pdflow.h"
 #include "../../include/pdflow_net.h"
 #include "pdflow_iterate.cuh"
@@ -108,6 +110,15 @@ int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, c
 int set_error_code(int code, const char* what, cudaError_t e = cudaSuccess);
 // The learned slot solve with every pair sent down the fallback path (the
 // serving lanes' graph warm-up uses it to capture the fallback graphs).
+// An NVTX range over a host-side scope (tracing: nsys / ncu --nvtx show the
+// library's calls and phases; without a tool attached it costs a function call).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 // Device bytes of the learned path's buffers (kept 60x80 solutions + second slot map).
 inline size_t learned_keep_bytes(unsigned batch)
 {

@@ -229,8 +229,13 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
         s->sol_keep = static_cast<float*>(p);
         s->map2 = reinterpret_cast<unsigned*>(static_cast<char*>(p) + keep);
     }
+    const NvtxRange trace_range("pdflow learned solve");
     LearnedCtx ctx{net, o.iter_scale, slots != nullptr};
-    int rc = run_graphed(s, n, scale_kind(o.iter_scale, slots != nullptr), learned_enqueue, &ctx, net);
+    int rc;
+    {
+        const NvtxRange head_range("head: plain to 60x80, network, warm 60x80");
+        rc = run_graphed(s, n, scale_kind(o.iter_scale, slots != nullptr), learned_enqueue, &ctx, net);
+    }
     if (rc) return rc;
     unsigned launches = s->launches;
     std::vector<float> e(2 * size_t(s->batch));
@@ -251,6 +256,7 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
         else keep.push_back(ids[k]);
     }
     // the head graph has finished (its energies were read), so both maps are free
+    const NvtxRange tail_range("continuations");
     if (!keep.empty()) {
         ce = cudaMemcpyAsync(s->map, keep.data(), sizeof(unsigned) * keep.size(), cudaMemcpyHostToDevice, s->stream);
         if (ce != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "H2D accepted slots", ce);

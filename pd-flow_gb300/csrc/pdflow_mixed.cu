@@ -200,6 +200,7 @@ int pdflow_push_frames_mixed(pdflow_solver* s, unsigned n, const unsigned* rows,
 
 int pdflow_solve_mixed(pdflow_solver* s, unsigned n)
 {
+    const NvtxRange trace_range("pdflow_solve_mixed");
     if (!s) {
         set_last_error("null handle");
         return PDFLOW_ERR_ARG;

@@ -106,6 +106,7 @@ void destroy_lane(Lane* L)
 // Runs one batch of a lane (outside the server lock).
 void run_batch(pdflow_server* srv, Lane* L, std::vector<Request*>& batch)
 {
+    const pdflow::NvtxRange trace_range("server lane batch");
     const unsigned n = unsigned(batch.size());
     const size_t img = size_t(L->width) * L->height;
     const size_t N = size_t(L->rows) * L->cols;

@@ -308,6 +308,9 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
         g.map = plan.map;
         const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];
         const float* seed = (i == plan.first) ? plan.seed : nullptr;
+        static const char* const kLevelNames[8] = {"level 0", "level 1", "level 2", "level 3",
+                                                   "level 4", "level 5", "level 6", "level 7"};
+        const NvtxRange level_range(kLevelNames[i < 8 ? i : 7]);
         cudaEvent_t* tr = plan.trace ? plan.trace + 3 * (i - plan.first) : nullptr;
         if (tr) CUDA_TRY(cudaEventRecord(tr[0], st), "trace event");
         CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st, seed), "level init launch");
@@ -535,6 +538,7 @@ size_t pdflow_device_bytes(const pdflow_solver* s)
 
 int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float* Z)
 {
+    const NvtxRange trace_range("pdflow_push_frames");
     if (!s || !I || !Z) return set_error(PDFLOW_ERR_ARG, "null argument");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
@@ -554,6 +558,7 @@ int pdflow_push_frame(pdflow_solver* s, const float* I, const float* Z) { return
 
 int pdflow_push_frames_u16_device(pdflow_solver* s, unsigned n, const uint8_t* d_intensity, const uint16_t* d_depth)
 {
+    const NvtxRange trace_range("pdflow_push_frames_u16_device");
     if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
@@ -623,6 +628,7 @@ int pdflow_push_frame_rgb8_mm(pdflow_solver* s, const uint8_t* rgb, const uint16
 
 int pdflow_solve_batch(pdflow_solver* s, unsigned n)
 {
+    const NvtxRange trace_range("pdflow_solve_batch");
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use pdflow_solve_slots");
@@ -634,6 +640,7 @@ int pdflow_solve(pdflow_solver* s) { return pdflow_solve_batch(s, 1); }
 
 int pdflow_read_flow_batch(pdflow_solver* s, unsigned n, float* dx, float* dy, float* dz)
 {
+    const NvtxRange trace_range("pdflow_read_flow_batch");
     if (!s || !dx || !dy || !dz) return set_error(PDFLOW_ERR_ARG, "null argument");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     const size_t b = size_t(s->rows) * s->cols * 4;
@@ -748,6 +755,7 @@ int pdflow_push_frames_slots_u16(pdflow_solver* s, unsigned n, const unsigned* s
 
 int pdflow_solve_slots(pdflow_solver* s, unsigned n, const unsigned* slots)
 {
+    const NvtxRange trace_range("pdflow_solve_slots");
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
     if (!s->slot_mode) return set_error(PDFLOW_ERR_STATE, "no frames were pushed per slot");
     int rc = upload_slots(s, n, slots);
