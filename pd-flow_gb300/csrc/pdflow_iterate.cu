@@ -21,6 +21,8 @@
 // Data written by another CTA is read with ld.global.cg (L2), never through a
 // possibly stale L1 line.  Per-pixel arithmetic is pdflow_math.cuh, identical
 // to the stage kernels, so the results are bit-for-bit the same.
+#include <atomic>
+
 #include <cooperative_groups.h>
 
 #include "pdflow_iterate.cuh"
@@ -260,8 +262,10 @@ __global__ void k_wait_probe(IterArgs a, unsigned limit)
     wait_neighbours(a, 1u, limit);
 }
 
-unsigned g_max_cluster = 8;    // largest cluster the GPU places with this kernel's resources
-unsigned g_max_dyn_smem = 0;   // dynamic shared memory available to the iteration kernels
+// Written by prepare_iterate (once per device, under the caller's lock), read by
+// planning threads: atomics, so concurrent handles never race on them.
+std::atomic<unsigned> g_max_cluster{8};    // largest cluster the GPU places with this kernel's resources
+std::atomic<unsigned> g_max_dyn_smem{0};   // dynamic shared memory available to the iteration kernels
 
 }  // namespace
 
@@ -275,7 +279,7 @@ IterPlan plan_iterate(LevelGeom g, int num_sms)
         pl.ctas = 1;
     } else if (g.N <= 19200) {
         pl.mode = kIterCluster;
-        pl.ctas = (g.C >= 160) ? g_max_cluster : 8;
+        pl.ctas = (g.C >= 160) ? g_max_cluster.load() : 8u;
     } else {
         pl.mode = kIterGrid;
         unsigned s = g.C / 2;
@@ -303,7 +307,8 @@ static cudaError_t allow_smem(int optin)
     cudaError_t e = cudaFuncGetAttributes(&fa, k_iterate<kMode>);
     if (e != cudaSuccess) return e;
     const int dyn = optin - (int)fa.sharedSizeBytes;
-    if (g_max_dyn_smem == 0 || (unsigned)dyn < g_max_dyn_smem) g_max_dyn_smem = (unsigned)dyn;
+    const unsigned cur = g_max_dyn_smem.load();
+    if (cur == 0 || (unsigned)dyn < cur) g_max_dyn_smem.store((unsigned)dyn);
     return cudaFuncSetAttribute(k_iterate<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
 }
 

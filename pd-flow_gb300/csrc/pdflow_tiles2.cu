@@ -19,6 +19,8 @@
 // pixels further out compute garbage from stale neighbours, exactly as they
 // would hold stale values if skipped, and no exact pixel ever reads them.  Reads beyond a region edge are redirected into the
 // region's own storage, so every shared access stays in bounds.
+#include <atomic>
+
 #include "pdflow_iterate.cuh"
 #include "pdflow_math.cuh"
 
@@ -499,7 +501,7 @@ static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 // 24x24 shape 9.4 % faster (73.6 -> 66.7 ms), the 40x34 shape 6 % faster
 // (77.3 -> 72.5 ms) and the 40x40 shape 10 % faster per iteration; bulk
 // stores gain nothing on top.
-static int g_copy_mode[4] = {1, 1, 1, 1};
+static std::atomic<int> g_copy_mode[4] = {{1}, {1}, {1}, {1}};   // set by a debug call, read by launchers
 
 void set_tile_copy_mode(int shape, int mode)
 {
