@@ -75,6 +75,15 @@ public:
         check(pdflow_push_frame_u16(handle_, intensity, depth), "pdflow_push_frame_u16");
     }
 
+    // Pushes an RGB-D camera frame as the live application reads it (row-major
+    // RGB888, uint16 depth in millimetres), converted on the device with that
+    // application's arithmetic (PD_flow_mrpt::CaptureFrame); rotate180 stores
+    // it in that loop's order.
+    void pushCameraFrame(const uint8_t* rgb, const uint16_t* depth_mm, bool rotate180 = true)
+    {
+        check(pdflow_push_frame_rgb8_mm(handle_, rgb, depth_mm, rotate180 ? 1 : 0), "pdflow_push_frame_rgb8_mm");
+    }
+
     bool loadRGBDFrames(const uint8_t* i1, const uint16_t* z1, const uint8_t* i2, const uint16_t* z2)
     {
         pushRawFrame(i1, z1);
