@@ -3,7 +3,7 @@ CUDA path (oracle/_ref/pdflow_ref.cubin through oracle/ref/refharness.c) on
 seeded synthetic RGB-D pairs.  Needs a GPU and the reference device code:
 
     make -C oracle/ref                      # where the reference sources exist
-    python tests/golden/make_golden.py --out gpurun_out/golden   # on a GPU
+    python tests/golden/make_golden.py --out golden_new   # on a GPU; then copy the .npz files here
 
 Each fixture stores the uint8/uint16 row-major input images (so the tests do
 not depend on the scene generator being bit-identical across machines) and the
@@ -52,7 +52,7 @@ def solve_case(rows, w, h, I1, Z1, I2, Z2, dump=False):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default="gpurun_out/golden")
+    ap.add_argument("--out", default="golden_new")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
 
