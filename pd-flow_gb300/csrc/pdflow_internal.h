@@ -87,6 +87,7 @@ struct SolvePlan {
     int energy_level = -1;               // after this level's median, its energy goes to ...
     float* energy = nullptr;             // ... device [pairs]
     const unsigned* map = nullptr;       // device [pairs] arena slots (null: slots 0..pairs-1)
+    bool all_steps = false;              // write the step-size planes even for levels run as tiles
     cudaEvent_t* trace = nullptr;        // eager runs only: 3 per solved level + 1, recorded before
                                          // each level's set-up, iterations and median, and at the end
 };

@@ -316,7 +316,9 @@ __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 }
 
 // performWarping (pdflow_cudalib.cu:629-652) + computeMu/computeStepSizes (:781-808).
-__global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p)
+// steps = false: only mu of the step fields (the tile kernels recompute the
+// step sizes from mu, ri, rj, ddu, ddv in registers).
+__global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p, bool steps)
 {
     const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     o = at(o, po);
@@ -341,6 +343,10 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
     L.ddt[index] = ddt;
     L.ddu[index] = ddu;
     L.ddv[index] = ddv;
+    if (!steps) {
+        L.mu[index] = data_weight(p.mu, ddu, ddv, ddt);
+        return;
+    }
     const float ri = L.ri[index], rj = L.rj[index];
     const float ri_m = (u > 0) ? L.ri[index - R] : 0.f;
     const float rj_m = (v > 0) ? L.rj[index - 1] : 0.f;
@@ -723,9 +729,10 @@ cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p, cudaStream_t st)
+cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p, cudaStream_t st,
+                              bool steps)
 {
-    k_warp_steps<<<level_grid(g), kBlock, 0, st>>>(g, old_l, new_l, L, p);
+    k_warp_steps<<<level_grid(g), kBlock, 0, st>>>(g, old_l, new_l, L, p, steps);
     return cudaGetLastError();
 }
 

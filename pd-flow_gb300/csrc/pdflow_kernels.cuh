@@ -131,8 +131,9 @@ cudaError_t launch_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L, cudaStr
 cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, double* part,
                           cudaStream_t st);
 cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st);
+// steps = false writes mu but not the 8 step-size planes (levels run as tiles).
 cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p,
-                              cudaStream_t st);
+                              cudaStream_t st, bool steps = true);
 cudaError_t launch_dual(LevelGeom g, LevelConsts L, State S, Params p, cudaStream_t st);
 cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old,
                           cudaStream_t st);

@@ -97,7 +97,7 @@ int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec
         if (r.kind == 0) {
             e = launch_level_init(g, r.step == 0, s->sol, o, n, s->L, s->S, st);
             if (e == cudaSuccess) e = launch_im_gradients(g, n, s->L, st);
-            if (e == cudaSuccess) e = launch_warp_steps(g, o, n, s->L, p, st);
+            if (e == cudaSuccess) e = launch_warp_steps(g, o, n, s->L, p, st, false);   // tiles only
             *count += 3;
             cur = s->S;
             nxt = alt;

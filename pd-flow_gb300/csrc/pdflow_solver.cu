@@ -180,6 +180,20 @@ LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, 
 // run as one launch (k_iterate: one CTA, one cluster, or, for a single pair,
 // the cooperative full grid) or, for a batch of pairs at a level that needs
 // the full grid, as two batched kernels per iteration.
+// Whether level `level`'s iterations run as shared-memory tiles (which
+// recompute the step sizes in registers).  Batches: tiles at every level
+// (measured faster than the cluster-persistent form from 15x20 up to 120x160
+// too); a single pair: tiles above 15x20 (per iteration at 30x40 .. 120x160
+// about half the time of the one-launch form; whole VGA solves 2.00 against
+// 2.34 ms, QVGA 1.22 against 1.55 ms), the one-CTA launch at 15x20.
+static bool level_runs_tiles(const pdflow_solver* s, const LevelGeom& g, unsigned iters, unsigned pairs,
+                             unsigned level)
+{
+    const int forced = level < 8 ? s->level_form[level] : -1;
+    if (forced >= 0) return forced >= 2 && iters > 0;
+    return s->iter_form >= 2 && iters > 0 && (pairs > 1 || g.N > 300u);
+}
+
 // Enqueues `iters` iterations of level i for pairs [0, pairs) in the
 // solve's launch form; returns the number of kernels launched via *count.
 // The final duals' buffer is reported in *fin.
@@ -191,19 +205,10 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
     const IterPlan pl = plan_iterate(g, s->num_sms);
     const int forced = level < 8 ? s->level_form[level] : -1;
     const bool one_launch_ok = (pairs == 1 || pl.mode != kIterGrid) && pl.smem_bytes <= iterate_smem_limit();
-    bool tiles, one_launch;
+    const bool tiles = level_runs_tiles(s, g, iters, pairs, level);
     const int form = forced >= 0 ? forced : s->iter_form;
-    if (forced >= 0) {
-        tiles = forced >= 2 && iters > 0;
-        one_launch = forced == 1 && iters > 0 && one_launch_ok;
-    } else {
-        // batches: tiles at every level (measured faster than the cluster-persistent form
-        // from 15x20 up to 120x160 too); a single pair: tiles above 15x20 (per iteration
-        // at 30x40 .. 120x160 about half the time of the one-launch form; whole VGA solves
-        // 2.00 against 2.34 ms, QVGA 1.22 against 1.55 ms), the one-CTA launch at 15x20
-        tiles = s->iter_form >= 2 && iters > 0 && (pairs > 1 || g.N > 300u);
-        one_launch = s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok;
-    }
+    const bool one_launch = forced >= 0 ? (forced == 1 && iters > 0 && one_launch_ok)
+                                        : (s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok);
     const bool paired = tiles && form >= 3;
     const int shape = form - 3;   // 40x40, 40x34, 24x24 or 24x28 tiles
     if (tiles) {
@@ -288,7 +293,7 @@ int enqueue_energy(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned l
     const PyrLevel o = s->pyr[s->new_slot ^ 1][li], n = s->pyr[s->new_slot][li];
     CUDA_TRY(launch_energy_prep(g, s->sol, s->L, st), "energy prep launch");
     CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
-    CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
+    CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st, false), "warping launch");   // the energy needs mu only
     CUDA_TRY(launch_energy(g, s->sol, s->L, p, out, s->energy_part, st), "energy launch");
     s->launches += 5;
     return PDFLOW_OK;
@@ -314,10 +319,11 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
         cudaEvent_t* tr = plan.trace ? plan.trace + 3 * (i - plan.first) : nullptr;
         if (tr) CUDA_TRY(cudaEventRecord(tr[0], st), "trace event");
         CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st, seed), "level init launch");
-        CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
-        CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st), "warping launch");
-        count += 3;
         const unsigned iters = scaled_iters(s->prm.num_max_iter[i], plan.iter_scale);
+        const bool steps = plan.all_steps || !level_runs_tiles(s, g, iters, pairs, i);
+        CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
+        CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st, steps), "warping launch");
+        count += 3;
         if (tr) CUDA_TRY(cudaEventRecord(tr[1], st), "trace event");
         State fin;
         int rc = enqueue_iterations(s, st, g, o, iters, pairs, &fin, &count, i);

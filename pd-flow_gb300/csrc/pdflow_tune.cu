@@ -72,6 +72,7 @@ int pdflow_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_t
     for (unsigned i = 0; i < s->ctf_levels && rc == PDFLOW_OK; ++i) {
         SolvePlan plan;
         plan.last = i;
+        plan.all_steps = true;   // every candidate form finds its step sizes
         rc = enqueue_solve(s, s->stream, n, plan);   // level i's constants in place
         if (rc) break;
         unsigned li;
