@@ -317,7 +317,9 @@ __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 
 // performWarping (pdflow_cudalib.cu:629-652) + computeMu/computeStepSizes (:781-808).
 // steps = false: only mu of the step fields (the tile kernels recompute the
-// step sizes from mu, ri, rj, ddu, ddv in registers).
+// step sizes from mu, ri, rj, ddu, ddv in registers); the free spd plane then
+// holds powf(ddt, 2) for the level's median, so each pixel's square is taken
+// once instead of once per neighbour.
 __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p, bool steps)
 {
     const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
@@ -345,6 +347,7 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
     L.ddv[index] = ddv;
     if (!steps) {
         L.mu[index] = data_weight(p.mu, ddu, ddv, ddt);
+        L.spd[index] = powf(ddt, 2.f);
         return;
     }
     const float ri = L.ri[index], rj = L.rj[index];
@@ -514,6 +517,7 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
     return median_lerp(cr, cl, med, fl, fr);
 }
 
+template <bool kDdtSq>   // L.spd holds powf(ddt, 2) (levels run as tiles)
 __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, State Salt, LevelSol out,
                          float* dx, float* dy, float* dz, Params p, int32_t* sel)
 {
@@ -543,7 +547,8 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
                 const int indr = (int)v + k, indc = (int)u + l;
                 const bool in = (indr >= 0) && (indr < (int)R) && (indc >= 0) && (indc < (int)C);
                 const int j = in ? (int)index + l * (int)R + k : (int)index;
-                const float pres = median_weight(depth_old, o.dep[j], L.ddt[j]);
+                const float pres = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
+                                          : median_weight(depth_old, o.dep[j], L.ddt[j]);
                 const float a = S.du[j], b = S.dv[j], c = S.dw[j];
                 // compact the present samples to the front, in the reference's order
 #pragma unroll
@@ -756,9 +761,14 @@ cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* de
 }
 
 cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out, float* dx,
-                          float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st, const State* alt)
+                          float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st, const State* alt,
+                          bool ddt_sq)
 {
-    k_median<<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p, sel);
+    if (ddt_sq)
+        k_median<true><<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p, sel);
+    else
+        k_median<false><<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p,
+                                                          sel);
     return cudaGetLastError();
 }
 

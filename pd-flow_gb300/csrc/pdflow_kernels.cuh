@@ -142,6 +142,6 @@ cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* de
 // carries kMapAlt (mixed batches); kMapFinest marks a pair's finest level.
 cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out,
                           float* dx, float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st,
-                          const State* alt = nullptr);
+                          const State* alt = nullptr, bool ddt_sq = false);   // ddt_sq: L.spd holds powf(ddt, 2)
 
 }  // namespace pdflow

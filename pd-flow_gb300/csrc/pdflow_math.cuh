@@ -291,6 +291,12 @@ __device__ __forceinline__ float median_weight(float z0, float z, float ddt)
     return qt(1.f, fm(10.f, powf(ddt, 2.f), fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
 }
 
+// The same weight from a precomputed ddt_sq = powf(ddt, 2.f).
+__device__ __forceinline__ float median_weight_sq(float z0, float z, float ddt_sq)
+{
+    return qt(1.f, fm(10.f, ddt_sq, fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
+}
+
 // Linear interpolation between the samples bracketing the weighted median
 // (pdflow_cudalib.cu:1109).
 __device__ __forceinline__ float median_lerp(float cum_r, float cum_l, float med, float f_l, float f_r)

@@ -107,7 +107,7 @@ int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec
             std::swap(cur, nxt);
             *count += 1;
         } else {
-            e = launch_median(g, false, o, s->L, s->S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st, &alt);
+            e = launch_median(g, false, o, s->L, s->S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st, &alt, true);
             *count += 1;
         }
         if (e != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "mixed batch launch", e);

@@ -333,7 +333,8 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
             ++count;
         }
         if (tr) CUDA_TRY(cudaEventRecord(tr[2], st), "trace event");
-        CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st),
+        CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st,
+                               nullptr, !steps),
                  "median launch");
         ++count;
         if (int(i) == plan.energy_level && plan.energy) {
