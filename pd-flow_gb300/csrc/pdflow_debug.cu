@@ -176,6 +176,7 @@ int pdflow_trace_solve(pdflow_solver* s, unsigned n, float* ms)
 {
     if (!s || !ms || n == 0 || n > s->batch) return fail(PDFLOW_ERR_ARG, "bad pair count or null output");
     if (s->slot_mode) return fail(PDFLOW_ERR_STATE, "frames were pushed per slot");
+    if (s->mixed) return fail(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (s->frames < 2) return fail(PDFLOW_ERR_STATE, "solve needs two pushed frames");
     const unsigned L = s->ctf_levels, ne = 3 * L + 1;
     std::vector<cudaEvent_t> ev(ne, nullptr);

@@ -167,6 +167,10 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
         set_last_error("null argument");
         return PDFLOW_ERR_ARG;
     }
+    if (s->mixed) {
+        set_last_error("a mixed-resolution handle: use the mixed calls");
+        return PDFLOW_ERR_STATE;
+    }
     if (n == 0 || n > s->batch || n > net_max_batch(net)) {
         set_last_error("pair count out of range (solver batch or network batch)");
         return PDFLOW_ERR_ARG;

@@ -547,6 +547,7 @@ int pdflow_push_frames(pdflow_solver* s, unsigned n, const float* I, const float
 {
     const NvtxRange trace_range("pdflow_push_frames");
     if (!s || !I || !Z) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     const size_t b = size_t(s->width) * s->height * 4;
@@ -567,6 +568,7 @@ int pdflow_push_frames_u16_device(pdflow_solver* s, unsigned n, const uint8_t* d
 {
     const NvtxRange trace_range("pdflow_push_frames_u16_device");
     if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     s->new_slot ^= 1;
@@ -600,6 +602,7 @@ int pdflow_push_frames_rgb8_mm_device(pdflow_solver* s, unsigned n, const uint8_
                                       int rotate180)
 {
     if (!s || !d_rgb || !d_depth_mm) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use the slot calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     s->new_slot ^= 1;
@@ -637,6 +640,7 @@ int pdflow_solve_batch(pdflow_solver* s, unsigned n)
 {
     const NvtxRange trace_range("pdflow_solve_batch");
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     if (s->slot_mode) return set_error(PDFLOW_ERR_STATE, "frames were pushed per slot: use pdflow_solve_slots");
     if (s->frames < 2) return set_error(PDFLOW_ERR_STATE, "solve needs two pushed frames");
@@ -649,6 +653,7 @@ int pdflow_read_flow_batch(pdflow_solver* s, unsigned n, float* dx, float* dy, f
 {
     const NvtxRange trace_range("pdflow_read_flow_batch");
     if (!s || !dx || !dy || !dz) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     const size_t b = size_t(s->rows) * s->cols * 4;
     CUDA_TRY(cudaMemcpy2DAsync(dx, b, s->dx, s->pair_stride, b, n, cudaMemcpyDeviceToHost, s->stream), "D2H dx");
@@ -674,6 +679,7 @@ int pdflow_flow_device(pdflow_solver* s, const float** dx, const float** dy, con
 int pdflow_copy_flow_device(pdflow_solver* s, unsigned n, float* d_dx, float* d_dy, float* d_dz)
 {
     if (!s || !d_dx || !d_dy || !d_dz) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (bad_count(s, n)) return set_error(PDFLOW_ERR_ARG, "pair count out of range");
     const size_t b = size_t(s->rows) * s->cols * 4;
     CUDA_TRY(cudaMemcpy2DAsync(d_dx, b, s->dx, s->pair_stride, b, n, cudaMemcpyDeviceToDevice, s->stream), "D2D dx");
@@ -726,6 +732,7 @@ int pdflow_push_frames_slots_u16_device(pdflow_solver* s, unsigned n, const unsi
                                         const uint8_t* d_intensity, const uint16_t* d_depth)
 {
     if (!s || !d_intensity || !d_depth) return set_error(PDFLOW_ERR_ARG, "null argument");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (!s->slot_mode && s->frames > 0)
         return set_error(PDFLOW_ERR_STATE, "frames were pushed for the whole batch: use the batch calls");
     int rc = upload_slots(s, n, slots);
@@ -764,6 +771,7 @@ int pdflow_solve_slots(pdflow_solver* s, unsigned n, const unsigned* slots)
 {
     const NvtxRange trace_range("pdflow_solve_slots");
     if (!s) return set_error(PDFLOW_ERR_ARG, "null handle");
+    if (s->mixed) return set_error(PDFLOW_ERR_STATE, "a mixed-resolution handle: use the mixed calls");
     if (!s->slot_mode) return set_error(PDFLOW_ERR_STATE, "no frames were pushed per slot");
     int rc = upload_slots(s, n, slots);
     if (rc) return rc;

@@ -44,3 +44,20 @@ def test_mixed_batch_rejects_bad_rows(built_lib):
         b.push([100], [i], [z])
     assert e.value.code == ERR_ARG
     b.close()
+
+
+def test_regular_calls_are_refused_on_a_mixed_handle(built_lib):
+    """A mixed-resolution handle answers PDFLOW_ERR_STATE to the single-shape
+    push / solve / read calls (its pairs have per-pair shapes)."""
+    from pdflow import _lib
+    lib = _lib.load()
+    import ctypes
+    h = ctypes.c_void_p()
+    assert lib.pdflow_create_mixed(4, ctypes.byref(h)) == _lib.OK
+    buf = np.zeros(640 * 480 * 4, np.float32)
+    assert lib.pdflow_solve_batch(h, 1) == _lib.ERR_STATE
+    assert lib.pdflow_push_frames(h, 1, buf.ctypes.data_as(ctypes.c_void_p), buf.ctypes.data_as(ctypes.c_void_p)) \
+        == _lib.ERR_STATE
+    assert lib.pdflow_read_flow_batch(h, 1, *[buf.ctypes.data_as(ctypes.c_void_p)] * 3) == _lib.ERR_STATE
+    assert "mixed" in _lib.last_error()
+    assert lib.pdflow_destroy(h) == _lib.OK
