@@ -586,7 +586,8 @@ def ours(args):
                        "l2": "batch working set far above L2 (no flush); plain single pair: L2 flushed per step",
                        "scenes": "seeded plane + 1-8 rigidly moving boxes/spheres, rendered on the GPU"},
             "accuracy": accuracy,
-            "batched": {"pairs_s": value, "p50_ms_per_batch": statistics.median(step_ms),
+            "batched": {"pairs_s": value, "step_ms": [round(x, 3) for x in step_ms],
+                        "p50_ms_per_batch": statistics.median(step_ms),
                         "p99_ms_per_batch": float(np.quantile(step_ms, 0.99))},
             "batched_plain": batched_plain, "plain_batch_trace": trace, "learned_half_iterations": learned_half,
             "mixed_batch": mixed,
