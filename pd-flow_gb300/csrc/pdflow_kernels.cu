@@ -449,50 +449,39 @@ __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* dep
 //
 // Stable sort of up to 9 samples (the reference's bubbleSortDev,
 // pdflow_cudalib.cu:1457-1473, swaps only on a strict '>', so equal values
-// keep their input order) as a 25-comparator sorting network on (value, input
-// index) keys (sort each triple, sort the columns of the 3x3 array, five
-// exchanges), which sorts every 0/1 input and hence every input; with the
-// index as tie-break the keys are distinct, so any sorting network yields
-// the stable order.  Missing samples (n < 9)
-// enter as (+inf, index >= n) and sort last.  Then the cumulative weights are
-// summed in sorted order, as the reference does, and the bracketing samples
-// are interpolated; the result and the selected index are the reference's bit
-// for bit.  Every index is a compile-time constant: nothing spills.
-__device__ __forceinline__ void cmp_swap(float& fa, float& wa, int& ia, float& fb, float& wb, int& ib)
-{
-    const bool s = (fb < fa) || (fb == fa && ib < ia);
-    const float tf = fa, tw = wa;
-    const int ti = ia;
-    fa = s ? fb : fa;
-    wa = s ? wb : wa;
-    ia = s ? ib : ia;
-    fb = s ? tf : fb;
-    wb = s ? tw : wb;
-    ib = s ? ti : ib;
-}
-
+// keep their input order) as an odd-even transposition network: 9 rounds of
+// exchanges between neighbours (i, i+1), i of the round's parity, each on a
+// strict '<'.  It sorts every 0/1 input and hence every input, and equal
+// values never pass each other, so the order is the stable one.  Missing
+// samples (n < 9) enter as (+inf, weight 0) after the present ones and stay
+// there.  Then the cumulative weights are summed in sorted order, as the
+// reference does, and the bracketing samples are interpolated; the result and
+// the selected index are the reference's bit for bit.  Every index is a
+// compile-time constant: nothing spills.
 __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned n, float med_or_neg,
                                          float* total, int32_t* cont_out)
 {
     float sf[9], sw[9];
-    int id[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const bool in = (unsigned)i < n;
         sf[i] = in ? f[i] : INFINITY;
         sw[i] = in ? w[i] : 0.f;
-        id[i] = i;
     }
-    // 25 comparators: sort the triples (0,1,2), (3,4,5), (6,7,8), sort the
-    // columns of the resulting 3x3 array, then the last five exchanges
-    constexpr int kNet[25][2] = {{0, 1}, {3, 4}, {6, 7}, {1, 2}, {4, 5}, {7, 8}, {0, 1}, {3, 4}, {6, 7},
-                                 {0, 3}, {3, 6}, {0, 3}, {1, 4}, {4, 7}, {1, 4}, {2, 5}, {5, 8}, {2, 5},
-                                 {1, 3}, {5, 7}, {2, 6}, {4, 6}, {2, 4}, {2, 3}, {5, 6}};
+    // odd-even transposition sort: 9 rounds of adjacent exchanges on a strict
+    // '<', so equal values never pass each other and the order is the stable
+    // one of the reference's bubble sort, without carrying input indices
 #pragma unroll
-    for (int c = 0; c < 25; ++c) {
-        const int a = kNet[c][0], b = kNet[c][1];
-        cmp_swap(sf[a], sw[a], id[a], sf[b], sw[b], id[b]);
-    }
+    for (int r = 0; r < 9; ++r)
+#pragma unroll
+        for (int a = r & 1; a + 1 < 9; a += 2) {
+            const bool sw_ = sf[a + 1] < sf[a];
+            const float tf = sf[a], tw = sw[a];
+            sf[a] = sw_ ? sf[a + 1] : sf[a];
+            sw[a] = sw_ ? sw[a + 1] : sw[a];
+            sf[a + 1] = sw_ ? tf : sf[a + 1];
+            sw[a + 1] = sw_ ? tw : sw[a + 1];
+        }
     float cum[9];
     cum[0] = sw[0];
 #pragma unroll

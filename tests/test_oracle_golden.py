@@ -121,32 +121,32 @@ def test_oracle_level_state_tracks_reference(golden_qvga, oracle_r60_dumps, fiel
 
 
 def test_median_sorting_network_sorts_every_zero_one_input():
-    """The 9-input comparator network of k_median (25 comparators: the
-    triples, the columns of the 3x3 array, five exchanges) sorts all 512 zero-one inputs, so
-    by the 0-1 principle it sorts every input; with (value, input index) keys
-    it reproduces the stable order of the reference's bubble sort."""
+    """The 9-input network of k_median (odd-even transposition: 9 rounds of
+    neighbour exchanges (i, i+1), i of the round's parity, on a strict '<')
+    sorts all 512 zero-one inputs, so by the 0-1 principle it sorts every
+    input; on ties it keeps the input order, the stable order of the
+    reference's bubble sort."""
     import itertools
-    import re
     src = open(os.path.join(os.path.dirname(__file__), "..", "pd-flow_gb300", "csrc", "pdflow_kernels.cu")).read()
-    body = src[src.index("kNet[25][2] = {"):]
-    body = body[:body.index("};")]
-    net = [tuple(map(int, m)) for m in re.findall(r"\{(\d+), (\d+)\}", body)]
-    assert len(net) == 25
+    assert "for (int r = 0; r < 9; ++r)" in src and "for (int a = r & 1; a + 1 < 9; a += 2)" in src
+    assert "const bool sw_ = sf[a + 1] < sf[a];" in src
+    net = [(a, a + 1) for r in range(9) for a in range(r & 1, 8, 2)]
+    assert len(net) == 36
     for bits in itertools.product((0, 1), repeat=9):
         x = list(bits)
         for a, b in net:
             if x[b] < x[a]:
                 x[a], x[b] = x[b], x[a]
         assert x == sorted(x)
-    # stable order on ties with (value, index) keys
+    # stable: with strict exchanges equal values keep their input order
     rng = np.random.default_rng(0)
-    for _ in range(200):
+    for _ in range(500):
         vals = rng.integers(0, 3, size=9).astype(float)
-        keys = [(v, i) for i, v in enumerate(vals)]
+        order = list(range(9))
         for a, b in net:
-            if keys[b] < keys[a]:
-                keys[a], keys[b] = keys[b], keys[a]
-        assert [i for _, i in keys] == sorted(range(9), key=lambda i: (vals[i], i))
+            if vals[order[b]] < vals[order[a]]:
+                order[a], order[b] = order[b], order[a]
+        assert order == sorted(range(9), key=lambda i: (vals[i], i))
 
 
 def test_live_app_rgb_decode_every_value():
