@@ -258,7 +258,7 @@ int pdflow_debug_wait_timeout(pdflow_solver* s, unsigned polls)
 
 int pdflow_set_tile_copy_mode(int shape, int mode)
 {
-    if (shape < 0 || shape > 3 || mode < 0 || mode > 3) return fail(PDFLOW_ERR_ARG, "shape 0..3, mode 0..3");
+    if (shape < 0 || shape > 3 || mode < 0 || mode > 7) return fail(PDFLOW_ERR_ARG, "shape 0..3, mode 0..7");
     set_tile_copy_mode(shape, mode);
     return PDFLOW_OK;
 }

@@ -42,6 +42,7 @@ struct LevelGeom {
     unsigned pairs = 1;
     size_t pstride = 0;
     const unsigned* map = nullptr;   // device [pairs]: arena slot of grid index y (null: slot y)
+    unsigned slots = 0;              // arena slots behind pstride (0: unknown)
 };
 
 // A map entry is an arena slot in its low 28 bits plus per-pair flags used by

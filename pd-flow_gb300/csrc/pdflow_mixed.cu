@@ -90,6 +90,7 @@ int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec
         LevelGeom g{R, C, R * C};
         g.pairs = r.count;
         g.pstride = s->pair_stride;
+        g.slots = s->batch;
         g.map = s->map_table + r.off;
         const unsigned li = kSteps - 1 - r.step;
         const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];

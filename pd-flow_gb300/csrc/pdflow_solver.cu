@@ -172,6 +172,7 @@ LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, 
     LevelGeom g{Ri, Ci, Ri * Ci};
     g.pairs = pairs;
     g.pstride = s->pair_stride;
+    g.slots = s->batch;
     return g;
 }
 

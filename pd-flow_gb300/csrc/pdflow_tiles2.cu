@@ -19,6 +19,8 @@
 // pixels further out compute garbage from stale neighbours, exactly as they
 // would hold stale values if skipped, and no exact pixel ever reads them.  Reads beyond a region edge are redirected into the
 // region's own storage, so every shared access stays in bounds.
+#include <cuda.h>
+
 #include <atomic>
 
 #include "pdflow_iterate.cuh"
@@ -62,6 +64,13 @@ struct Tile2Args {
     bool bulk;            // region columns load by TMA bulk copies (16-byte aligned: R % 4 == 0)
     bool bulk_store;      // interior columns store by TMA bulk copies
     unsigned* status;     // device word: kTileBulkTimeout when the bounded wait for the region gives up
+    bool tensor;          // 24x24 shape: each plane's 32x32 region by one TMA tensor copy (maps below)
+};
+
+// Tensor maps of the 24 region planes (3D: rows, columns, arena slots), for
+// the tensor-copy region load of the 24x24 shape.
+struct Tile2Maps {
+    CUtensorMap m[T_NPLANES];
 };
 
 constexpr unsigned kTileBulkTimeout = 0x54494C45u;
@@ -123,12 +132,12 @@ __device__ __forceinline__ void clamp_pd(float& pd)
 
 template <int TV, int TU>
 __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlocksPerSM)
-    k_iterate_tiles2(Tile2Args a)
+    k_iterate_tiles2(Tile2Args a, const __grid_constant__ Tile2Maps tm)
 {
     using S = Shape<TV, TU>;
     constexpr int kTV = S::kTV, kRV = S::kRV, kPV = S::kPV;
     constexpr int kTU = S::kTU, kRU = S::kRU, kPlane = S::kPlane, kCols = S::kCols, kTY = S::kTY;
-    extern __shared__ __align__(16) float sm[];
+    extern __shared__ __align__(128) float sm[];   // TMA tensor copies land on 128-byte boundaries
     const size_t po = pair_off(a.g.map, a.g.pstride, blockIdx.y);
     const LevelConsts L = at(a.L, po);
     const State src = at(a.src, po), dst = at(a.dst, po);
@@ -168,14 +177,30 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
         // one bulk copy per (plane, region column): RV contiguous floats, all
         // addresses and sizes multiples of 16 bytes (checked by the launcher)
         const uint32_t b = smem_addr(&bar);
-        const uint32_t bytes = (uint32_t)(T_NPLANES * RU * RV) * 4u;
+        constexpr bool kTensorShape = TV == 24 && TU == 24;   // 32x32 regions = one tensor box per plane
+        const bool tensor = kTensorShape && a.tensor;
+        // tensor copies move whole 32x32 boxes (rows or columns past the level's
+        // edge arrive as zeros and, like rows beyond the region, are never read)
+        const uint32_t bytes = tensor ? (uint32_t)(T_NPLANES * kPlane) * 4u : (uint32_t)(T_NPLANES * RU * RV) * 4u;
         if (threadIdx.x == 0) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+            if (tensor) {
+                // one copy per plane: box (32 rows, 32 columns, 1 slot) at (rv0, ru0, slot);
+                // rv0 is a multiple of 4 floats (16 bytes), as tensor copies require
+                const int slot = (int)(a.g.map ? (__ldg(a.g.map + blockIdx.y) & kMapSlotMask) : blockIdx.y);
+#pragma unroll
+                for (int k = 0; k < T_NPLANES; ++k)
+                    asm volatile(
+                        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(sm + k * kPlane)),
+                        "l"(reinterpret_cast<uint64_t>(&tm.m[k])), "r"(rv0), "r"(ru0), "r"(slot), "r"(b)
+                        : "memory");
+            }
         }
         __syncthreads();
-        for (int c = threadIdx.x; c < T_NPLANES * RU; c += blockDim.x) {
+        for (int c = threadIdx.x; !tensor && c < T_NPLANES * RU; c += blockDim.x) {
             const int k = c / RU, ru = c % RU;
             const float* g = s_gs[k] + (size_t)rv0 + (size_t)(ru0 + ru) * R;
             asm volatile(
@@ -484,28 +509,30 @@ cudaError_t prepare_tiles2()
 }
 
 template <int TV, int TU>
-static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st)
+static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st, const Tile2Maps& maps)
 {
     using S = Shape<TV, TU>;
     a.tiles_v = (g.R + TV - 1) / TV;
     dim3 grid(a.tiles_v * ((g.C + TU - 1) / TU), g.pairs);
-    k_iterate_tiles2<TV, TU><<<grid, S::kThreads, sizeof(float) * T_NPLANES * S::kPlane, st>>>(a);
+    k_iterate_tiles2<TV, TU><<<grid, S::kThreads, sizeof(float) * T_NPLANES * S::kPlane, st>>>(a, maps);
     return cudaGetLastError();
 }
 
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // Which region copies use TMA bulk copies, per shape: bit 0 = load, bit 1 =
-// store; index 0 = 40x40 tiles, 1 = 40x34 tiles, 2 = 24x24, 3 = 24x28.  Measured
+// store, bit 2 (24x24 only, with bit 0) = the load as one tensor copy per
+// plane instead of one bulk copy per plane column; index 0 = 40x40 tiles,
+// 1 = 40x34 tiles, 2 = 24x24, 3 = 24x28.  Measured
 // on 64 VGA pairs (whole batched solves, one GB300): bulk loads make the
 // 24x24 shape 9.4 % faster (73.6 -> 66.7 ms), the 40x34 shape 6 % faster
 // (77.3 -> 72.5 ms) and the 40x40 shape 10 % faster per iteration; bulk
 // stores gain nothing on top.
-static std::atomic<int> g_copy_mode[4] = {{1}, {1}, {1}, {1}};   // set by a debug call, read by launchers
+static std::atomic<int> g_copy_mode[4] = {{1}, {1}, {5}, {1}};   // set by a debug call, read by launchers
 
 void set_tile_copy_mode(int shape, int mode)
 {
-    if (shape >= 0 && shape < 4) g_copy_mode[shape] = mode & 3;
+    if (shape >= 0 && shape < 4) g_copy_mode[shape] = mode & 7;
 }
 
 cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
@@ -534,11 +561,29 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
     a.bulk = ok && (mode & 1);
     a.bulk_store = ok && (mode & 2);
     a.status = status;
+    a.tensor = false;
+    Tile2Maps local{};   // a launch parameter: copied at launch (and into a graph node when captured)
+    if (shape == 2 && a.bulk && (mode & 4) && g.slots > 0) {
+        // 3D maps (rows, columns, arena slots) of the 24 region planes, box 32 x 32 x 1
+        const float* tp[T_NPLANES] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd, src.puu, src.puv,
+                                      src.pvu, src.pvv, src.pwu, src.pwv, L.mu, L.ddt, L.ddu, L.ddv, L.dct,
+                                      L.dcu, L.dcv, L.ri, L.rj, L.du_prev, L.dv_prev};
+        const cuuint64_t dims[3] = {g.R, g.C, g.slots};
+        const cuuint64_t strides[2] = {cuuint64_t(g.R) * 4u, g.pstride};
+        const cuuint32_t box[3] = {32, 32, 1}, estr[3] = {1, 1, 1};
+        bool enc = true;
+        for (int k = 0; k < T_NPLANES && enc; ++k)
+            enc = cuTensorMapEncodeTiled(&local.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(tp[k]),
+                                         dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        a.tensor = enc;   // else the per-column bulk copies
+    }
     switch (shape) {
-    case 0: return launch_shape<40, 40>(a, g, st);
-    case 1: return launch_shape<40, 34>(a, g, st);
-    case 2: return launch_shape<24, 24>(a, g, st);
-    case 3: return launch_shape<24, 28>(a, g, st);
+    case 0: return launch_shape<40, 40>(a, g, st, local);
+    case 1: return launch_shape<40, 34>(a, g, st, local);
+    case 2: return launch_shape<24, 24>(a, g, st, local);
+    case 3: return launch_shape<24, 28>(a, g, st, local);
     default: return cudaErrorInvalidValue;
     }
 }
