@@ -74,10 +74,11 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
  * tiles (iteration form 3), 1 = 40x34 tiles (form 4), 2 = 24x24 tiles
  * (form 5), 3 = 24x28 tiles (form 6); mode bit 0 = TMA bulk
  * copies for the region load, bit 1 = for the interior store, else plain
- * loads/stores; bit 2 (24x24 tiles, with bit 0) = the region load as one TMA
- * tensor copy per plane (a 32x32 box through a 3D tensor map of rows,
- * columns and arena slots) instead of one bulk copy per plane column.  Levels whose row count is not a multiple of 4 always use
- * plain loads and stores.  All modes give the same bits. */
+ * loads/stores; bit 2 (with bit 0) = the region load as one TMA tensor copy
+ * per plane (the whole region as one box through a 3D tensor map of rows,
+ * columns and arena slots) instead of one bulk copy per plane column.
+ * Levels whose row count is not a multiple of 4 always use plain loads and
+ * stores.  All modes give the same bits. */
 int pdflow_set_tile_copy_mode(int shape, int mode);
 
 /* Per-level, per-phase timing of a plain solve of pairs [0, n) (tracing; no

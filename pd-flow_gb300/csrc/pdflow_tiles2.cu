@@ -64,11 +64,11 @@ struct Tile2Args {
     bool bulk;            // region columns load by TMA bulk copies (16-byte aligned: R % 4 == 0)
     bool bulk_store;      // interior columns store by TMA bulk copies
     unsigned* status;     // device word: kTileBulkTimeout when the bounded wait for the region gives up
-    bool tensor;          // 24x24 shape: each plane's 32x32 region by one TMA tensor copy (maps below)
+    bool tensor;          // each plane's kRV x kRU region by one TMA tensor copy (maps below)
 };
 
 // Tensor maps of the 24 region planes (3D: rows, columns, arena slots), for
-// the tensor-copy region load of the 24x24 shape.
+// the tensor-copy region load (box = one whole region).
 struct Tile2Maps {
     CUtensorMap m[T_NPLANES];
 };
@@ -177,9 +177,8 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
         // one bulk copy per (plane, region column): RV contiguous floats, all
         // addresses and sizes multiples of 16 bytes (checked by the launcher)
         const uint32_t b = smem_addr(&bar);
-        constexpr bool kTensorShape = TV == 24 && TU == 24;   // 32x32 regions = one tensor box per plane
-        const bool tensor = kTensorShape && a.tensor;
-        // tensor copies move whole 32x32 boxes (rows or columns past the level's
+        const bool tensor = a.tensor;
+        // tensor copies move whole kRV x kRU boxes (rows or columns past the level's
         // edge arrive as zeros and, like rows beyond the region, are never read)
         const uint32_t bytes = tensor ? (uint32_t)(T_NPLANES * kPlane) * 4u : (uint32_t)(T_NPLANES * RU * RV) * 4u;
         if (threadIdx.x == 0) {
@@ -187,7 +186,7 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
             if (tensor) {
-                // one copy per plane: box (32 rows, 32 columns, 1 slot) at (rv0, ru0, slot);
+                // one copy per plane: box (kRV rows, kRU columns, 1 slot) at (rv0, ru0, slot);
                 // rv0 is a multiple of 4 floats (16 bytes), as tensor copies require
                 const int slot = (int)(a.g.map ? (__ldg(a.g.map + blockIdx.y) & kMapSlotMask) : blockIdx.y);
 #pragma unroll
@@ -508,10 +507,50 @@ cudaError_t prepare_tiles2()
     return e;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry-point query, so
+// that the library does not link the driver library itself (it then loads,
+// for symbol checks, on machines without a GPU driver); null: not available.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled()
+{
+    static const EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
 template <int TV, int TU>
-static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st, const Tile2Maps& maps)
+static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st, bool want_tensor)
 {
     using S = Shape<TV, TU>;
+    Tile2Maps maps{};   // a launch parameter: copied at launch (and into a graph node when captured)
+    a.tensor = false;
+    const EncodeTiledFn encode = want_tensor ? encode_tiled() : nullptr;
+    if (encode) {
+        // 3D maps (rows, columns, arena slots) of the 24 region planes, box = the whole region
+        const float* tp[T_NPLANES] = {a.src.du,  a.src.dv,  a.src.dw,  a.src.dua, a.src.dva, a.src.dwa,
+                                      a.src.pd,  a.src.puu, a.src.puv, a.src.pvu, a.src.pvv, a.src.pwu,
+                                      a.src.pwv, a.L.mu,    a.L.ddt,   a.L.ddu,   a.L.ddv,   a.L.dct,
+                                      a.L.dcu,   a.L.dcv,   a.L.ri,    a.L.rj,    a.L.du_prev, a.L.dv_prev};
+        const cuuint64_t dims[3] = {g.R, g.C, g.slots};
+        const cuuint64_t strides[2] = {cuuint64_t(g.R) * 4u, g.pstride};
+        const cuuint32_t box[3] = {S::kRV, S::kRU, 1}, estr[3] = {1, 1, 1};
+        bool enc = true;
+        for (int k = 0; k < T_NPLANES && enc; ++k)
+            enc = encode(&maps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(tp[k]), dims, strides,
+                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        a.tensor = enc;   // else the per-column bulk copies
+    }
     a.tiles_v = (g.R + TV - 1) / TV;
     dim3 grid(a.tiles_v * ((g.C + TU - 1) / TU), g.pairs);
     k_iterate_tiles2<TV, TU><<<grid, S::kThreads, sizeof(float) * T_NPLANES * S::kPlane, st>>>(a, maps);
@@ -521,13 +560,14 @@ static cudaError_t launch_shape(Tile2Args a, const LevelGeom& g, cudaStream_t st
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // Which region copies use TMA bulk copies, per shape: bit 0 = load, bit 1 =
-// store, bit 2 (24x24 only, with bit 0) = the load as one tensor copy per
-// plane instead of one bulk copy per plane column; index 0 = 40x40 tiles,
+// store, bit 2 (with bit 0) = the load as one tensor copy per plane
+// instead of one bulk copy per plane column; index 0 = 40x40 tiles,
 // 1 = 40x34 tiles, 2 = 24x24, 3 = 24x28.  Measured
 // on 64 VGA pairs (whole batched solves, one GB300): bulk loads make the
 // 24x24 shape 9.4 % faster (73.6 -> 66.7 ms), the 40x34 shape 6 % faster
 // (77.3 -> 72.5 ms) and the 40x40 shape 10 % faster per iteration; bulk
-// stores gain nothing on top.
+// stores gain nothing on top; tensor loads make the 24x24 shape another
+// 6.4 % faster than its bulk loads (65.38 -> 61.19 ms).
 static std::atomic<int> g_copy_mode[4] = {{1}, {1}, {5}, {1}};   // set by a debug call, read by launchers
 
 void set_tile_copy_mode(int shape, int mode)
@@ -561,29 +601,15 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
     a.bulk = ok && (mode & 1);
     a.bulk_store = ok && (mode & 2);
     a.status = status;
-    a.tensor = false;
-    Tile2Maps local{};   // a launch parameter: copied at launch (and into a graph node when captured)
-    if (shape == 2 && a.bulk && (mode & 4) && g.slots > 0) {
-        // 3D maps (rows, columns, arena slots) of the 24 region planes, box 32 x 32 x 1
-        const float* tp[T_NPLANES] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd, src.puu, src.puv,
-                                      src.pvu, src.pvv, src.pwu, src.pwv, L.mu, L.ddt, L.ddu, L.ddv, L.dct,
-                                      L.dcu, L.dcv, L.ri, L.rj, L.du_prev, L.dv_prev};
-        const cuuint64_t dims[3] = {g.R, g.C, g.slots};
-        const cuuint64_t strides[2] = {cuuint64_t(g.R) * 4u, g.pstride};
-        const cuuint32_t box[3] = {32, 32, 1}, estr[3] = {1, 1, 1};
-        bool enc = true;
-        for (int k = 0; k < T_NPLANES && enc; ++k)
-            enc = cuTensorMapEncodeTiled(&local.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(tp[k]),
-                                         dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-        a.tensor = enc;   // else the per-column bulk copies
-    }
+    // tensor copies: one per plane, the region as one box; its first row
+    // (a multiple of 4) and the row stride (R % 4 == 0) are 16-byte aligned,
+    // and every shape's plane size in shared memory is a multiple of 128 bytes
+    const bool want_tensor = a.bulk && (mode & 4) && g.slots > 0;
     switch (shape) {
-    case 0: return launch_shape<40, 40>(a, g, st, local);
-    case 1: return launch_shape<40, 34>(a, g, st, local);
-    case 2: return launch_shape<24, 24>(a, g, st, local);
-    case 3: return launch_shape<24, 28>(a, g, st, local);
+    case 0: return launch_shape<40, 40>(a, g, st, want_tensor);
+    case 1: return launch_shape<40, 34>(a, g, st, want_tensor);
+    case 2: return launch_shape<24, 24>(a, g, st, want_tensor);
+    case 3: return launch_shape<24, 28>(a, g, st, want_tensor);
     default: return cudaErrorInvalidValue;
     }
 }

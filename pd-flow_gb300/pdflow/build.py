@@ -82,7 +82,7 @@ def build(verbose: bool = False) -> str:
     if _stale(LIB_PATH, objs):
         cuda_lib = os.path.join(_cuda_home(), "lib64")
         cmd = [_nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB_PATH, *objs,
-               "-Xlinker", f"-rpath,{cuda_lib}", "-lcuda", "-lpthread"]
+               "-Xlinker", f"-rpath,{cuda_lib}", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -50,7 +50,7 @@ def test_tile_copy_modes_give_the_same_bits(built_lib, form):
     n = 4
     pairs = [scenes.make_pair(950 + k) for k in range(n)]
     out = []
-    for mode in (0, 1, 2, 3, 5, 7) if form == 5 else range(4):   # 24x24: also the tensor-copy load
+    for mode in (0, 1, 2, 3, 5, 7):   # plain, bulk and tensor-copy loads, plain and bulk stores
         assert lib.pdflow_set_tile_copy_mode(form - 3, mode) == 0
         b = BatchSolver(240, 320, 240, n, iteration_form=form)
         b.push_raw(np.stack([p[0] for p in pairs]), np.stack([p[1] for p in pairs]))
