@@ -28,7 +28,9 @@ to 60x80, network seed, scaled iterations from 60x80 on, energy fallback).
 from __future__ import annotations
 
 import argparse
+import contextlib
 import ctypes
+import gc
 import json
 import os
 import statistics
@@ -93,7 +95,17 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def wait_first(self, timeout_s: float = 5.0):
+        """Waits (bounded) for nvidia-smi's first sample, so that its start-up
+        is over before a timed region begins; returns the sample count."""
+        t_end = time.monotonic() + timeout_s
+        while self.proc is not None and not self.lines and time.monotonic() < t_end:
+            time.sleep(0.02)
+        return len(self.lines)
+
+    def stop(self, since: int = 0):
+        """Ends sampling; summarises the samples from index `since` on (those
+        taken during the timed region), or all of them if none came after."""
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -103,7 +115,8 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        lines = self.lines[since:] if len(self.lines) > since else self.lines
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 7:
                 continue
@@ -119,6 +132,22 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+@contextlib.contextmanager
+def paused_gc():
+    """Python's cyclic garbage collector paused inside a timed loop: a full
+    collection of the interpreter's heap is a host stall of tens of ms, which
+    leaves the device idle where a step waits for the host (the learned path's
+    fallback decision)."""
+    gc.collect()
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
 
 
 # ---------------------------------------------------------------------------
@@ -324,6 +353,8 @@ def ours(args):
         push()
         return b.solve_learned(B, net, scale, margin)
 
+    sampler = ClockSampler(local)
+    sampler.start()   # nvidia-smi starts up during the warm-up, not in the timed region
     with torch.cuda.stream(stream):
         for _ in range(W):
             step()
@@ -333,14 +364,13 @@ def ours(args):
     launches_per_step = 2 * 6 + cnt.value      # 2 pushes x (decode + 5 pyramid levels) + the learned solve
     if ws > 1:
         torch.distributed.barrier()
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
+    sampler.wait_first()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     t_all0, t_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     fallbacks = 0
-    with torch.cuda.stream(stream):
+    mark = len(sampler.lines)
+    with paused_gc(), torch.cuda.stream(stream):
         t_all0.record(stream)
         for k in range(K):
             ev[k][0].record(stream)
@@ -349,7 +379,7 @@ def ours(args):
         t_all1.record(stream)
     b.synchronize()
     torch.cuda.synchronize()
-    clocks = sampler.stop()
+    clocks = sampler.stop(mark)
     step_ms = [a.elapsed_time(e) for a, e in ev]
     value, total_ms = replica_value(torch, t_all0.elapsed_time(t_all1), B, K, device=dev)
     learned = b.read_flow(B)
@@ -393,7 +423,7 @@ def ours(args):
     # the learned warm start with the finer levels' iterations halved (the
     # schedule's nominal setting), same handle, frames and fallback rule
     half = 0.5
-    with torch.cuda.stream(stream):
+    with paused_gc(), torch.cuda.stream(stream):
         for _ in range(2):
             push()
             b.solve_learned(B, net, half, margin)
@@ -461,7 +491,7 @@ def ours(args):
     torch.cuda.synchronize()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
+    with paused_gc(), torch.cuda.stream(stream):
         t0.record(stream)
         for _ in range(ke):
             e2e_step()
@@ -521,9 +551,10 @@ def ours(args):
     pipelined(2)
     torch.cuda.synchronize()
     p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    p0.record(copy)
-    pipelined(ke)
-    p1.record(copy)
+    with paused_gc():
+        p0.record(copy)
+        pipelined(ke)
+        p1.record(copy)
     torch.cuda.synchronize()
     pipe_ms = p0.elapsed_time(p1)
     e2e = {"value": ws * B * ke / (pipe_ms / 1000.0), "unit": "pairs/s",

@@ -566,9 +566,10 @@ static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 // on 64 VGA pairs (whole batched solves, one GB300): bulk loads make the
 // 24x24 shape 9.4 % faster (73.6 -> 66.7 ms), the 40x34 shape 6 % faster
 // (77.3 -> 72.5 ms) and the 40x40 shape 10 % faster per iteration; bulk
-// stores gain nothing on top; tensor loads make the 24x24 shape another
-// 6.4 % faster than its bulk loads (65.38 -> 61.19 ms).
-static std::atomic<int> g_copy_mode[4] = {{1}, {1}, {5}, {1}};   // set by a debug call, read by launchers
+// stores gain nothing on top; tensor loads make every shape another 8-10 %
+// faster than its bulk loads (24x24: 66.42 -> 61.25 ms, 40x40: 68.7 ->
+// 63.7 ms, 40x34: 71.0 -> 65.7 ms, 24x28: 68.4 -> 62.3 ms).
+static std::atomic<int> g_copy_mode[4] = {{5}, {5}, {5}, {5}};   // set by a debug call, read by launchers
 
 void set_tile_copy_mode(int shape, int mode)
 {

@@ -39,7 +39,7 @@ def test_autotuned_forms_give_the_same_bits(built_lib):
     b.close()
 
 
-DEFAULT_COPY_MODE = {3: 1, 4: 1, 5: 5, 6: 1}   # the library's defaults (pdflow_tiles2.cu)
+DEFAULT_COPY_MODE = {3: 5, 4: 5, 5: 5, 6: 5}   # the library's defaults (pdflow_tiles2.cu)
 
 
 @pytest.mark.parametrize("form", [3, 4, 5, 6])
