@@ -160,7 +160,10 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
     const float* gs[T_NPLANES] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd, src.puu, src.puv,
                                   src.pvu, src.pvv, src.pwu, src.pwv, L.mu, L.ddt, L.ddu, L.ddv, L.dct, L.dcu,
                                   L.dcv, L.ri, L.rj, L.du_prev, L.dv_prev};
-    __shared__ __align__(8) unsigned long long bar;
+    // bar[0]: the whole region, or with tensor copies only the five planes the
+    // step-size set-up reads (mu, ddu, ddv, ri, rj); bar[1]: with tensor copies
+    // the other 19 planes, awaited after the set-up so that it overlaps them
+    __shared__ __align__(8) unsigned long long bar[2];
     __shared__ const float* s_gs[T_NPLANES];
     __shared__ float* s_gd[13];
     // plane tables of the bulk copies; the barrier after the load publishes them
@@ -173,41 +176,8 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
 #pragma unroll
         for (int k = 0; k < 13; ++k) s_gd[k] = gd[k];
     }
-    if (a.bulk) {
-        // one bulk copy per (plane, region column): RV contiguous floats, all
-        // addresses and sizes multiples of 16 bytes (checked by the launcher)
-        const uint32_t b = smem_addr(&bar);
-        const bool tensor = a.tensor;
-        // tensor copies move whole kRV x kRU boxes (rows or columns past the level's
-        // edge arrive as zeros and, like rows beyond the region, are never read)
-        const uint32_t bytes = tensor ? (uint32_t)(T_NPLANES * kPlane) * 4u : (uint32_t)(T_NPLANES * RU * RV) * 4u;
-        if (threadIdx.x == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
-            if (tensor) {
-                // one copy per plane: box (kRV rows, kRU columns, 1 slot) at (rv0, ru0, slot);
-                // rv0 is a multiple of 4 floats (16 bytes), as tensor copies require
-                const int slot = (int)(a.g.map ? (__ldg(a.g.map + blockIdx.y) & kMapSlotMask) : blockIdx.y);
-#pragma unroll
-                for (int k = 0; k < T_NPLANES; ++k)
-                    asm volatile(
-                        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(sm + k * kPlane)),
-                        "l"(reinterpret_cast<uint64_t>(&tm.m[k])), "r"(rv0), "r"(ru0), "r"(slot), "r"(b)
-                        : "memory");
-            }
-        }
-        __syncthreads();
-        for (int c = threadIdx.x; !tensor && c < T_NPLANES * RU; c += blockDim.x) {
-            const int k = c / RU, ru = c % RU;
-            const float* g = s_gs[k] + (size_t)rv0 + (size_t)(ru0 + ru) * R;
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    smem_addr(sm + k * kPlane + ru * kRV)),
-                "l"(g), "r"((uint32_t)RV * 4u), "r"(b)
-                : "memory");
-        }
+    // bounded wait for phase 0 of an mbarrier; on timeout the status word is set
+    auto wait_region = [&](uint32_t b) {
         bool done = false;
         for (uint32_t i = 0; i < kBulkWaitLimit && !done; ++i) {
             uint32_t ok;
@@ -220,6 +190,55 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
             done = ok != 0;
         }
         if (!done && a.status) atomicExch(a.status, kTileBulkTimeout);
+    };
+    const bool tensor = a.bulk && a.tensor;
+    if (a.bulk) {
+        // one bulk copy per (plane, region column): RV contiguous floats, all
+        // addresses and sizes multiples of 16 bytes (checked by the launcher)
+        const uint32_t b = smem_addr(&bar[0]), b1 = smem_addr(&bar[1]);
+        // tensor copies move whole kRV x kRU boxes (rows or columns past the level's
+        // edge arrive as zeros and, like rows beyond the region, are never read)
+        constexpr uint32_t kBox = (uint32_t)kPlane * 4u;
+        const uint32_t bytes = tensor ? 5u * kBox : (uint32_t)(T_NPLANES * RU * RV) * 4u;
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
+            if (tensor) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b1));
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+            if (tensor) {
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b1),
+                             "r"((uint32_t)(T_NPLANES - 5) * kBox)
+                             : "memory");
+                // one copy per plane: box (kRV rows, kRU columns, 1 slot) at (rv0, ru0, slot);
+                // rv0 is a multiple of 4 floats (16 bytes), as tensor copies require.
+                // The set-up's planes go first.
+                const int slot = (int)(a.g.map ? (__ldg(a.g.map + blockIdx.y) & kMapSlotMask) : blockIdx.y);
+                constexpr int kOrder[T_NPLANES] = {T_MU,  T_DDU, T_DDV, T_RI,  T_RJ,  T_DU,  T_DV,  T_DW,
+                                                   T_UA,  T_VA,  T_WA,  T_PD,  T_PUU, T_PUV, T_PVU, T_PVV,
+                                                   T_PWU, T_PWV, T_DDT, T_DCT, T_DCU, T_DCV, T_DUP, T_DVP};
+#pragma unroll
+                for (int o = 0; o < T_NPLANES; ++o) {
+                    const int k = kOrder[o];
+                    asm volatile(
+                        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(sm + k * kPlane)),
+                        "l"(reinterpret_cast<uint64_t>(&tm.m[k])), "r"(rv0), "r"(ru0), "r"(slot),
+                        "r"(o < 5 ? b : b1)
+                        : "memory");
+                }
+            }
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; !tensor && c < T_NPLANES * RU; c += blockDim.x) {
+            const int k = c / RU, ru = c % RU;
+            const float* g = s_gs[k] + (size_t)rv0 + (size_t)(ru0 + ru) * R;
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_addr(sm + k * kPlane + ru * kRV)),
+                "l"(g), "r"((uint32_t)RV * 4u), "r"(b)
+                : "memory");
+        }
+        wait_region(b);
     } else {
 #pragma unroll
         for (int c = 0; c < kCols; ++c) {
@@ -305,6 +324,7 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
 #pragma unroll
         for (int m = 0; m < 8; ++m) sg[c][m] = make_float2(s[0][m], s[1][m]);
     }
+    if (tensor) wait_region(smem_addr(&bar[1]));   // the state and the other constant planes
     const float2 li2 = make_float2(li, li), ld2v = make_float2(ld, ld), two = make_float2(2.f, 2.f);
     const float2 zero = make_float2(0.f, 0.f);
 
