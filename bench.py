@@ -286,7 +286,8 @@ def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
         srv = Server(device_budget_bytes=64 << 30, slots_per_lane=2, learned=learned,
                      iter_scale=iter_scale if learned else 1.0, energy_margin=margin,
                      net_params=weights if learned else None)
-        infos, _, summary = simulate(srv, streams_used, rate_hz=rate, seed=1)
+        with paused_gc():   # the load generator keeps its arrival schedule
+            infos, _, summary = simulate(srv, streams_used, rate_hz=rate, seed=1)
         lat = {r: [i["done_ms"] - i["submit_ms"] for i in infos
                    if i["has_flow"] and streams_used[i["stream_id"]][1] == r] for r in (240, 480)}
         st = srv.stats()

@@ -19,6 +19,11 @@
 // pixels further out compute garbage from stale neighbours, exactly as they
 // would hold stale values if skipped, and no exact pixel ever reads them.  Reads beyond a region edge are redirected into the
 // region's own storage, so every shared access stays in bounds.
+//
+// Region loads (levels with rows % 4 == 0): each plane's whole region as one
+// TMA tensor copy (3D tensor map over rows, columns and arena slots), issued by
+// one thread and completing on two mbarriers (the step-size set-up's five
+// planes first); or one TMA bulk copy per plane column; or plain loads.
 #include <cuda.h>
 
 #include <atomic>

@@ -88,19 +88,22 @@ def simulate(server: Server, streams, rate_hz: float = 30.0, seed: int = 0, want
     (intensity, depth) numpy pairs.  Each stream's frames arrive as a Poisson
     process of rate `rate_hz` (exponential gaps).  Returns per-request infos
     and a summary: p50 / p99 latency of the frames that produced a flow,
-    aggregate flows per second over the run, batch sizes."""
+    aggregate flows per second over the run, batch sizes, and how late the
+    submissions ran against their scheduled arrival times (a late load
+    generator bunches arrivals into bursts)."""
     rng = np.random.default_rng(seed)
     sids = [server.open_stream(w, h) for w, h, _ in streams]
     heap = []
     t0 = time.perf_counter()
     for j, (_, _, frames) in enumerate(streams):
         heapq.heappush(heap, (rng.exponential(1.0 / rate_hz), j, 0))
-    pending = []
+    pending, late = [], []
     while heap:
         t_arr, j, k = heapq.heappop(heap)
         now = time.perf_counter() - t0
         if t_arr > now:
             time.sleep(t_arr - now)
+        late.append((time.perf_counter() - t0 - t_arr) * 1e3)
         frames = streams[j][2]
         rid = server.submit(sids[j], *frames[k])
         pending.append((rid, sids[j]))
@@ -122,6 +125,8 @@ def simulate(server: Server, streams, rate_hz: float = 30.0, seed: int = 0, want
                    flows_per_s=flows / (span_ms / 1e3) if span_ms > 0 else None,
                    mean_batch_pairs=float(np.mean([i["batch_pairs"] for i in infos if i["has_flow"]])) if flows else 0,
                    wall_s=wall, errors=int(sum(1 for i in infos if i["status"] != 0)),
+                   arrival_lateness_p99_ms=float(np.percentile(late, 99)) if late else None,
+                   arrival_lateness_max_ms=float(max(late)) if late else None,
                    fallbacks=int(server.stats()["fallbacks"]))
     for sid in sids:
         server.close_stream(sid)
