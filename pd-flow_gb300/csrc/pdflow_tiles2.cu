@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(Shape<TV, TU>::kThreads, Shape<TV, TU>::kBlock
             }
         }
     }
-    __syncthreads();
+    // plain loads need a barrier before any thread reads its neighbours; TMA copies
+    // are visible to every thread once its own wait on their mbarrier has returned
+    if (!a.bulk) __syncthreads();
 
     const float li = a.p.lambda_i, ld = a.p.lambda_d;
     unsigned flags[kCols];
