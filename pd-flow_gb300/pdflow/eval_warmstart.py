@@ -1,4 +1,4 @@
-"""Judges the learned warm start against the plain solver on held-out pairs.
+"""Evaluates the learned warm start against the plain solver on held-out pairs.
 
     python -m pdflow.eval_warmstart --weights warmstart.npz --rows 480 --pairs 64 --scales 0.5
 
