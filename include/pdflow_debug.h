@@ -77,8 +77,9 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
  * loads/stores; bit 2 (with bit 0) = the region load as one TMA tensor copy
  * per plane (the whole region as one box through a 3D tensor map of rows,
  * columns and arena slots) instead of one bulk copy per plane column.
- * Levels whose row count is not a multiple of 4 always use plain loads and
- * stores.  All modes give the same bits. */
+ * Default: mode 5 (tensor-copy loads, plain stores) for every shape.  Levels
+ * whose row count is not a multiple of 4 always use plain loads and stores.
+ * All modes give the same bits. */
 int pdflow_set_tile_copy_mode(int shape, int mode);
 
 /* Per-level, per-phase timing of a plain solve of pairs [0, n) (tracing; no
