@@ -98,6 +98,68 @@ __device__ __forceinline__ void stage_tile(unsigned char* dst, const __nv_bfloat
     }
 }
 
+// The pixel of an A row gathered by ConvGather: each thread stages the same
+// row of every A tile (kThreads == kBM), so its (b, y, x) is found once.
+struct ConvRow {
+    int b, y, x;
+    bool valid;
+};
+
+__device__ __forceinline__ ConvRow conv_row(const ConvGather& cv, int gr, int nrows)
+{
+    ConvRow cr;
+    const int hw = cv.H * cv.W;
+    cr.valid = gr < nrows;
+    cr.b = gr / hw;
+    const int rr = gr - cr.b * hw;
+    cr.y = rr / cv.W;
+    cr.x = rr - cr.y * cv.W;
+    return cr;
+}
+
+// stage_tile for an A operand that is the im2col of a 3x3 convolution
+// (ConvGather): each 16-byte piece is 8 channels of one tap of this thread's
+// pixel, read from the NHWC source, or zero-filled outside the image, past
+// row nrows or past K, exactly the values the materialised im2col holds.
+__device__ __forceinline__ void stage_conv_tile(unsigned char* dst, const ConvGather& cv, const ConvRow& cr, int k0,
+                                                int K)
+{
+    static_assert(kThreads == kBM, "one A row per thread");
+    const __nv_bfloat16* s1 = static_cast<const __nv_bfloat16*>(cv.s1);
+    const __nv_bfloat16* s2 = static_cast<const __nv_bfloat16*>(cv.s2);
+    const int cin = cv.c1 + cv.c2;
+    const int HH = cv.up1 ? cv.H1 : cv.H, WW = cv.up1 ? cv.W1 : cv.W;
+    const int r = threadIdx.x;
+    int tap = k0 / cin, ch = k0 - tap * cin;   // of piece 0; pieces step 8 channels
+#pragma unroll
+    for (int kc = 0; kc < kBK / 8; ++kc) {
+        const int gk = k0 + kc * 8;
+        const __nv_bfloat16* g = s1;   // read nothing (source size 0)
+        bool in = cr.valid && gk < K;
+        if (in) {
+            const int h = cr.y + tap / 3 - 1, w = cr.x + tap % 3 - 1;
+            in = h >= 0 && h < cv.H && w >= 0 && w < cv.W;
+            if (in) {
+                if (ch < cv.c1) {
+                    const int hh = cv.up1 ? h / 2 : h, ww = cv.up1 ? w / 2 : w;
+                    g = s1 + (((size_t)cr.b * HH + hh) * WW + ww) * cv.c1 + ch;
+                } else {
+                    g = s2 + (((size_t)cr.b * cv.H + h) * cv.W + w) * cv.c2 + (ch - cv.c1);
+                }
+            }
+        }
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                         smem_u32(dst + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16)),
+                     "l"(g), "r"(in ? 16 : 0)
+                     : "memory");
+        ch += 8;
+        if (ch >= cin) {
+            ch -= cin;
+            ++tap;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -131,12 +193,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
     bool ok = true;
 
     const __nv_bfloat16* A = static_cast<const __nv_bfloat16*>(a.A);
+    const ConvRow crow = a.conv_a ? conv_row(a.conv, m0 + (int)threadIdx.x, a.M) : ConvRow{0, 0, 0, false};
     const __nv_bfloat16* B = static_cast<const __nv_bfloat16*>(a.B);
     // prologue: chunks 0 .. kStages-2, one commit group each (empty past the end)
 #pragma unroll
     for (int i = 0; i < kStages - 1; ++i) {
         if (i < nk) {
-            stage_tile(sA(i), A, a.lda, m0, kBM, a.M, kbeg + i * kBK, kend);
+            if (a.conv_a) stage_conv_tile(sA(i), a.conv, crow, kbeg + i * kBK, kend);
+            else stage_tile(sA(i), A, a.lda, m0, kBM, a.M, kbeg + i * kBK, kend);
             stage_tile(sB(i), B, a.ldb, n0, a.bn, a.N, kbeg + i * kBK, kend);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
@@ -172,7 +236,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
         if (nc < nk) {
             const int ns = nc % kStages;
             if (kc >= 1) ok &= mbar_wait(smem_u32(&mbar[ns]), uint32_t(((kc - 1) / kStages) & 1));
-            stage_tile(sA(ns), A, a.lda, m0, kBM, a.M, kbeg + nc * kBK, kend);
+            if (a.conv_a) stage_conv_tile(sA(ns), a.conv, crow, kbeg + nc * kBK, kend);
+            else stage_tile(sA(ns), A, a.lda, m0, kBM, a.M, kbeg + nc * kBK, kend);
             stage_tile(sB(ns), B, a.ldb, n0, a.bn, a.N, kbeg + nc * kBK, kend);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");

@@ -11,6 +11,17 @@ constexpr unsigned kGemmTimeout = 0x47454D4Du;   // status word written when a b
 // (lda, ldb and K multiples of 8); C fp32 or bf16 with leading dimension ldc.
 // k_per_split < K splits K over grid.z (fp32 output only): split z writes its
 // partial to C + z * split_stride.
+// The A operand gathered while staging, as the im2col of a 3x3 "same"
+// convolution, instead of read from a materialised [M][K] matrix: row p =
+// pixel (b, y, x) of an n x H x W batch, column k = tap * (c1 + c2) + channel
+// over [src1 (nearest-upsampled from H1 x W1 when up1) | src2], NHWC bf16 with
+// channel counts multiples of 8 (16-byte pieces never straddle a tap).
+struct ConvGather {
+    const void* s1 = nullptr;
+    const void* s2 = nullptr;
+    int c1 = 0, c2 = 0, up1 = 0, H1 = 0, W1 = 0, H = 0, W = 0;
+};
+
 struct GemmArgs {
     const void* A = nullptr;
     const void* B = nullptr;
@@ -25,6 +36,8 @@ struct GemmArgs {
     int k_per_split = 0;          // 0: no split
     size_t split_stride = 0;      // elements
     unsigned* status = nullptr;   // device word, kGemmTimeout on a bounded-wait timeout
+    int conv_a = 0;               // 1: A is conv's im2col (A, lda unused)
+    ConvGather conv;
 };
 
 cudaError_t prepare_gemm_tc();

@@ -61,7 +61,7 @@ struct pdflow_solver {
         unsigned pairs;
         int form;
         unsigned kind;                   // which enqueue sequence (plain, slot-mapped, learned ...)
-        const void* key;                 // object the sequence reads (the network), or null
+        unsigned long long key;          // identity of the object the sequence reads (the network's uid), or 0
         cudaGraphExec_t exec;
         unsigned launches;
     };
@@ -107,7 +107,7 @@ unsigned scaled_iters(unsigned iters, float scale);
 // equal ctx contents.
 using EnqueueFn = int (*)(pdflow_solver* s, cudaStream_t st, unsigned pairs, const void* ctx);
 int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx,
-                const void* key = nullptr);
+                unsigned long long key = 0);
 int set_error_code(int code, const char* what, cudaError_t e = cudaSuccess);
 // The learned slot solve with every pair sent down the fallback path (the
 // serving lanes' graph warm-up uses it to capture the fallback graphs).

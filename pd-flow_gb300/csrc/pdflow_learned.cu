@@ -106,7 +106,7 @@ int learned_enqueue(pdflow_solver* s, cudaStream_t st, unsigned pairs, const voi
     if (!rc) rc = net_seed(c.net, int(pairs), net_input_buffer(c.net), s->seed);
     net_set_stream_internal(c.net, net_st);
     if (rc) return rc;
-    total += 2 + 3 * 12 + 3 + 2;   // gather, input, 12 x (im2col + GEMM), 3 pools, head bias + output
+    total += 1 + net_seed_launches(c.net, int(pairs));   // the input gather, then the network
 
     SolvePlan warm;
     warm.first = kSeedLevel;
@@ -238,7 +238,10 @@ int learned_solve(pdflow_solver* s, unsigned n, const unsigned* slots, pdflow_ne
     int rc;
     {
         const NvtxRange head_range("head: plain to 60x80, network, warm 60x80");
-        rc = run_graphed(s, n, scale_kind(o.iter_scale, slots != nullptr), learned_enqueue, &ctx, net);
+        // keyed by the network's uid, never by its address: a network created
+        // where a destroyed one lived must not replay that one's graph (whose
+        // launches point at the destroyed network's buffers)
+        rc = run_graphed(s, n, scale_kind(o.iter_scale, slots != nullptr), learned_enqueue, &ctx, net_uid(net));
     }
     if (rc) return rc;
     unsigned launches = s->launches;

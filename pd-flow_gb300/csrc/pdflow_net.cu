@@ -18,6 +18,7 @@
 //   dec1: [up(dec2) 32 | skip1 16] -> 16     80x60
 //   head: 16 -> 3 (padded to 16), no ReLU, FP32 output
 // 3x3 convolutions with zero padding; 338 k parameters.
+#include <atomic>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -382,6 +383,7 @@ struct Act {
 }  // namespace
 
 struct pdflow_net {
+    unsigned long long uid = 0;      // unique per created network (key of graphs that read it)
     unsigned max_batch = 0;
     cudaStream_t stream = nullptr;
     std::vector<Act> act;
@@ -552,6 +554,13 @@ T* dalloc(pdflow_net* n, size_t count, cudaError_t* e)
     return static_cast<T*>(p);
 }
 
+// From this many inputs on, a convolution's GEMM gathers its im2col operand
+// while staging it (no im2col kernel, no column matrix round trip: 48.06 ->
+// 47.73 ms per 64-pair learned VGA solve); below it the separate im2col kernel
+// is faster (one pair: 2.035 against 2.083 ms), as the small GEMM is
+// latency-bound.  Both give the same bits.
+constexpr int kImplicitConvMinBatch = 16;
+
 int conv_forward(pdflow_net* n, const Conv& c, size_t ci, int nb)
 {
     cudaStream_t st = n->stream;
@@ -560,11 +569,25 @@ int conv_forward(pdflow_net* n, const Conv& c, size_t ci, int nb)
     const Act* a2 = c.src2 >= 0 ? &n->act[c.src2] : nullptr;
     const size_t P = size_t(nb) * c.H * c.W;
     const int K = c.K();
-    k_im2col<<<blocks(P * 9 * (K / 72)), 256, 0, st>>>(a1.x, c.c1, c.up1, a1.H, a1.W, a2 ? a2->x : nullptr, c.c2, nb,
-                                                       c.H, c.W, n->col);
-    NET_TRY(cudaGetLastError(), "im2col launch");
     GemmArgs g;
-    g.A = n->col;
+    if (nb >= kImplicitConvMinBatch) {
+        g.conv_a = 1;
+        g.conv.s1 = a1.x;
+        g.conv.s2 = a2 ? a2->x : nullptr;
+        g.conv.c1 = c.c1;
+        g.conv.c2 = c.c2;
+        g.conv.up1 = c.up1;
+        g.conv.H1 = a1.H;
+        g.conv.W1 = a1.W;
+        g.conv.H = c.H;
+        g.conv.W = c.W;
+        g.A = a1.x;
+    } else {
+        k_im2col<<<blocks(P * 9 * (K / 72)), 256, 0, st>>>(a1.x, c.c1, c.up1, a1.H, a1.W, a2 ? a2->x : nullptr,
+                                                           c.c2, nb, c.H, c.W, n->col);
+        NET_TRY(cudaGetLastError(), "im2col launch");
+        g.A = n->col;
+    }
     g.B = n->Wb[ci];
     g.M = int(P);
     g.N = c.cout_pad;
@@ -797,6 +820,13 @@ int net_gather_input(pdflow_net* n, const PyrLevel& o, const PyrLevel& nw, size_
 
 float* net_input_buffer(pdflow_net* n) { return n->input; }
 unsigned net_max_batch(const pdflow_net* n) { return n->max_batch; }
+unsigned long long net_uid(const pdflow_net* n) { return n->uid; }
+unsigned net_seed_launches(const pdflow_net* n, int nb)
+{
+    // input, per convolution (im2col +) GEMM, pools, head bias, head output
+    const unsigned convs = unsigned(n->conv.size());
+    return 1u + convs * (nb >= kImplicitConvMinBatch ? 1u : 2u) + unsigned(n->pools.size()) + 2u;
+}
 cudaStream_t net_stream(const pdflow_net* n) { return n->stream; }
 void net_set_stream_internal(pdflow_net* n, cudaStream_t st) { n->stream = st; }
 
@@ -820,6 +850,8 @@ int pdflow_net_create(unsigned max_batch, unsigned long long seed, pdflow_net** 
         return net_fail(PDFLOW_ERR_NO_DEVICE, "this library is built for sm_103a (GB300) only");
     NET_TRY(prepare_gemm_once(), "GEMM kernel attributes");
     pdflow_net* n = new (std::nothrow) pdflow_net();
+    static std::atomic<unsigned long long> next_uid{1};
+    if (n) n->uid = next_uid++;
     if (!n) return net_fail(PDFLOW_ERR_OOM, "host allocation");
     n->max_batch = max_batch;
     build_graph(n);

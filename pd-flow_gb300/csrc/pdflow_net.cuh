@@ -21,6 +21,10 @@ cudaError_t launch_gather_seed_input(const PyrLevel& old_l, const PyrLevel& new_
 // the network's stream.
 int net_seed(pdflow_net* n, int nb, const float* input, float* seed);
 unsigned net_max_batch(const pdflow_net* n);
+// Unique per network created in this process (never reused, unlike addresses).
+unsigned long long net_uid(const pdflow_net* n);
+// Kernel launches of net_seed for nb inputs.
+unsigned net_seed_launches(const pdflow_net* n, int nb);
 cudaStream_t net_stream(const pdflow_net* n);
 void net_set_stream_internal(pdflow_net* n, cudaStream_t st);
 

@@ -350,7 +350,8 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
     return PDFLOW_OK;
 }
 
-int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx, const void* key)
+int run_graphed(pdflow_solver* s, unsigned pairs, unsigned kind, EnqueueFn fn, const void* ctx,
+                unsigned long long key)
 {
     if (!s->use_graph) return fn(s, s->stream, pairs, ctx);
     cudaGraphExec_t ge = nullptr;

@@ -62,6 +62,26 @@ def test_forward_matches_oracle(torch):
     net.close()
 
 
+def test_gathered_convolutions_equal_the_im2col_ones(torch):
+    """From 16 inputs on the convolution GEMMs gather their im2col operand while
+    staging it; below 16 a separate im2col kernel builds it.  Each output row
+    of a GEMM accumulates the same products in the same order either way, so
+    20 inputs in one forward equal the same inputs in forwards of 4, bit for bit."""
+    n, chunk = 20, 4
+    net = Net(n, seed=3)
+    net.set_params(no.init_params(5))
+    inp, _ = _batch(2, n)
+    d_in = torch.from_numpy(inp).cuda()
+    whole = torch.zeros((n, 3, no.HW), dtype=torch.float32, device="cuda")
+    net.forward(n, d_in.data_ptr(), whole.data_ptr())
+    parts = torch.zeros((n, 3, no.HW), dtype=torch.float32, device="cuda")
+    for k in range(0, n, chunk):
+        net.forward(chunk, d_in[k:k + chunk].data_ptr(), parts[k:k + chunk].data_ptr())
+    torch.cuda.synchronize()
+    net.close()
+    assert np.array_equal(whole.cpu().numpy().view(np.uint32), parts.cpu().numpy().view(np.uint32))
+
+
 def test_gradients_match_oracle(torch):
     """GPU gradients against the oracle with the same bf16 rounding points.  The
     GPU's FP32 accumulation flips some bf16 roundings, so the tolerance is
