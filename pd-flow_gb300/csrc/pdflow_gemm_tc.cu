@@ -29,9 +29,12 @@ namespace {
 constexpr int kBM = 128, kBK = 64, kMaxBN = 128, kThreads = 128;
 constexpr uint32_t kTmemCols = 128;
 constexpr int kStageA = kBM * kBK * 2;         // 16 KB
-constexpr int kStageB = kMaxBN * kBK * 2;      // 16 KB
+constexpr int kStageB = kMaxBN * kBK * 2;      // 16 KB at the widest N tile
 constexpr int kStages = 3;
-constexpr int kSmemBytes = kStages * (kStageA + kStageB) + 64;
+constexpr int kSmemBytes = kStages * (kStageA + kStageB) + 64;   // the attribute: the largest launch
+// A launch's B stages hold only its N tile (bn rows), so narrow GEMMs fit
+// more CTAs per SM (bn = 16: 55 KB, four CTAs, 4 x 128 TMEM columns = 512).
+constexpr int smem_bytes(int bn) { return kStages * (kStageA + bn * kBK * 2) + 64; }
 constexpr uint32_t kWaitLimit = 1u << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -165,8 +168,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_tc(GemmArgs a)
     extern __shared__ __align__(1024) unsigned char smem[];
     // stage i: A at smem + i * kStageA, B after all A stages
     auto sA = [&](int i) { return smem + i * kStageA; };
-    auto sB = [&](int i) { return smem + kStages * kStageA + i * kStageB; };
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kStages * (kStageA + kStageB));
+    const int stage_b = a.bn * kBK * 2;
+    auto sB = [&](int i) { return smem + kStages * kStageA + i * stage_b; };
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kStages * (kStageA + stage_b));
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + kStages);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * a.bn;
@@ -323,7 +327,7 @@ cudaError_t launch_gemm_tc(const GemmArgs& args, cudaStream_t st)
     const unsigned splits = (unsigned)((a.K + a.k_per_split - 1) / a.k_per_split);
     if (splits > 1 && a.out_bf16) return cudaErrorInvalidValue;
     dim3 grid((a.M + kBM - 1) / kBM, (a.N + a.bn - 1) / a.bn, splits);
-    k_gemm_tc<<<grid, kThreads, kSmemBytes, st>>>(a);
+    k_gemm_tc<<<grid, kThreads, smem_bytes(a.bn), st>>>(a);
     return cudaGetLastError();
 }
 
