@@ -77,3 +77,5 @@ def test_simulator_submits_every_frame_in_stream_order_and_summarises():
     assert all(v == list(range(6)) for v in per_stream.values())
     assert summary["p50_ms"] == pytest.approx(5.0) and summary["p99_ms"] == pytest.approx(5.0)
     assert summary["errors"] == 0 and sorted(fake.closed) == [0, 1, 2]
+    # submissions never precede their scheduled arrival; lateness is reported
+    assert 0.0 <= summary["arrival_lateness_p99_ms"] <= summary["arrival_lateness_max_ms"]
