@@ -4,26 +4,36 @@
 Workload: VGA scene flow, rows = 480 (640x480 frames, 6 pyramid levels),
 seeded synthetic RGB-D pairs (textured plane plus 1-8 boxes/spheres with
 rigid motions, depth noise and 2 % holes) rendered on the GPU.  A step is one
-pass of the hot path over one batch: push both frames of every pair (device
-decode + Gaussian pyramid) and the learned warm-started solve (plain levels
-to 60x80, network seed, scaled iterations from 60x80 on, energy fallback).
+pass of the hot path over one batch of 64 pairs: push both frames of every
+pair (device decode + Gaussian pyramid) and solve them.
 
-  value      learned + batched VGA pairs/s, frames resident in HBM (per-step
-             CUDA events on the solver's stream; ~90 MB of state per pair, far
+  value      VGA pairs/s of the fastest batched configuration whose mean
+             end-point error against the plain result is <= 1 mm (the
+             metric's accuracy bar): the plain schedule (bit-exact with the
+             reference) or the learned warm start, whichever is faster among
+             those that meet the bar; frames resident in HBM, per-step CUDA
+             events on the solver's stream (~90 MB of state per pair, far
              larger than L2, so no flush is needed)
-  accuracy   end-point error against the plain result and against the scenes'
-             ground-truth motion, energy relative to the plain solve
-  e2e        the same through the public C ABI from pinned host buffers: raw
-             frames host->device, solve, flow device->host, every step
+  candidates every batched configuration measured, with its pairs/s and its
+             end-point error against the plain result
+  learned    the learned warm start (60x80 seed, scaled iterations, energy
+             fallback): pairs/s, accuracy against the plain result, the
+             scenes' ground-truth motion and the energy the iterations minimise
+  e2e        the headline configuration through the public C ABI from pinned
+             host buffers: raw frames host->device, solve, flow device->host
+             every step
   plain      one pair at a time (the plain single-pair solver), L2 flushed
-             before every step; pairs/s and p50/p99 latency
-  serving    16 simulated cameras through the request loop: p50/p99 latency
+             before every step; pairs/s, p50/p99 latency, per-level L2 rate
+  serving    simulated cameras through the request loop, at several loads
   roofline   the dominant kernel: the finest level's iterations, timed alone
   cpu_baseline / --impl reference
              the FP32 C/OpenMP restatement of the reference (oracle/) on the
              host cores, on a bounded sample of the same workload
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
+
+--gpus N outside torchrun starts N replica processes itself (one per GPU,
+127.0.0.1 rendezvous), as torchrun would.
 """
 from __future__ import annotations
 
@@ -332,7 +342,7 @@ def ours(args):
     net = Net(B)
     net.set_params(weights)
 
-    # ---------------- learned + batched, frames resident in HBM ----------------
+    # ---------------- batched configurations, frames resident in HBM ----------------
     b = BatchSolver(ROWS, WIDTH, HEIGHT, B)
     _lib.check(lib.pdflow_set_stream(b.handle, ctypes.c_void_p(stream.cuda_stream)), "pdflow_set_stream")
 
@@ -350,63 +360,89 @@ def ours(args):
         plain_b = b.read_flow(B)
         e_plain = b.energy(B)
 
-    def step():
+    def plain_step():
         push()
-        return b.solve_learned(B, net, scale, margin)
+        b.solve(B)
+        return 0
+
+    def learned_step():
+        push()
+        return b.solve_learned(B, net, scale, margin)["fallbacks"]
 
     sampler = ClockSampler(local)
     sampler.start()   # nvidia-smi starts up during the warm-up, not in the timed region
-    with torch.cuda.stream(stream):
-        for _ in range(W):
-            step()
-    b.synchronize()
-    cnt = ctypes.c_uint()
-    _lib.check(lib.pdflow_last_solve_launches(b.handle, ctypes.byref(cnt)), "launch count")
-    launches_per_step = 2 * 6 + cnt.value      # 2 pushes x (decode + 5 pyramid levels) + the learned solve
-    if ws > 1:
-        torch.distributed.barrier()
+
+    def timed(step):
+        """W untimed steps, then K steps bracketed by a barrier and a device
+        synchronisation, each between CUDA events on the solver's stream.
+        Returns (all ranks' pairs/s, slowest rank's ms, per-step ms, launches
+        per step, fallbacks)."""
+        with torch.cuda.stream(stream):
+            for _ in range(W):
+                step()
+        b.synchronize()
+        cnt = ctypes.c_uint()
+        _lib.check(lib.pdflow_last_solve_launches(b.handle, ctypes.byref(cnt)), "launch count")
+        if ws > 1:
+            torch.distributed.barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        t_all0, t_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        fb = 0
+        with paused_gc(), torch.cuda.stream(stream):
+            t_all0.record(stream)
+            for k in range(K):
+                ev[k][0].record(stream)
+                fb += step()
+                ev[k][1].record(stream)
+            t_all1.record(stream)
+        b.synchronize()
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        v, tot = replica_value(torch, t_all0.elapsed_time(t_all1), B, K, device=dev)
+        # 2 pushes x (decode + 5 pyramid levels) + the solve's own launches
+        return v, tot, [a_.elapsed_time(e_) for a_, e_ in ev], 2 * 6 + cnt.value, fb
+
     sampler.wait_first()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    t_all0, t_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    fallbacks = 0
     mark = len(sampler.lines)
-    with paused_gc(), torch.cuda.stream(stream):
-        t_all0.record(stream)
-        for k in range(K):
-            ev[k][0].record(stream)
-            fallbacks += step()["fallbacks"]
-            ev[k][1].record(stream)
-        t_all1.record(stream)
-    b.synchronize()
-    torch.cuda.synchronize()
+    plain_value, plain_total, plain_steps, plain_launches, _ = timed(plain_step)
+    plain_timed = b.read_flow(B)
+    learned_value, learned_total, learned_steps, learned_launches, fallbacks = timed(learned_step)
     clocks = sampler.stop(mark)
-    step_ms = [a.elapsed_time(e) for a, e in ev]
-    value, total_ms = replica_value(torch, t_all0.elapsed_time(t_all1), B, K, device=dev)
     learned = b.read_flow(B)
     e_learned = b.energy(B)
-    ep_plain = epe(learned, plain_b, valid)
-    accuracy = {"iter_scale": scale, "energy_margin": margin, "fallbacks_per_step": fallbacks / K,
-                "epe_vs_plain_mm": float(ep_plain.mean() * 1e3), "epe_vs_plain_max_pair_mm": float(ep_plain.max() * 1e3),
-                "epe_bar_mm": 1.0, "epe_bar_met": bool(ep_plain.mean() <= 1e-3),
-                "epe_vs_ground_truth_mm": {"learned": float(epe(learned, gt, valid).mean() * 1e3),
-                                           "plain": float(epe(plain_b, gt, valid).mean() * 1e3)},
-                "energy_ratio_to_plain": float((e_learned / e_plain).mean())}
-
-    # plain batched on the same handle (the schedule without the network)
-    with torch.cuda.stream(stream):
-        for _ in range(2):
-            push()
-            b.solve(B)
-        b.synchronize()
-        ta, tb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ta.record(stream)
-        for _ in range(max(3, K // 2)):
-            push()
-            b.solve(B)
-        tb.record(stream)
-    torch.cuda.synchronize()
-    batched_plain = {"pairs_s": B * max(3, K // 2) / (ta.elapsed_time(tb) / 1000.0), "epe_vs_plain_mm": 0.0}
+    ep_plain_run = epe(plain_timed, plain_b, valid)
+    ep_learned = epe(learned, plain_b, valid)
+    bar_m = 1e-3
+    candidates = [
+        {"config": "plain schedule, batched (autotuned launch forms)", "kind": "plain", "pairs_s": plain_value,
+         "ms_per_step": plain_total / K, "epe_vs_plain_mm": float(ep_plain_run.mean() * 1e3),
+         "bit_exact_with_plain": all(np.array_equal(x.view(np.uint32), y.view(np.uint32))
+                                     for x, y in zip(plain_timed, plain_b))},
+        {"config": f"learned warm start at 60x80, {scale:g}x iterations, {margin:g} energy fallback, batched",
+         "kind": "learned", "pairs_s": learned_value, "ms_per_step": learned_total / K,
+         "epe_vs_plain_mm": float(ep_learned.mean() * 1e3)}]
+    for c in candidates:
+        c["meets_epe_bar"] = c["epe_vs_plain_mm"] <= bar_m * 1e3
+    head = max((c for c in candidates if c["meets_epe_bar"]), key=lambda c: c["pairs_s"])
+    value, total_ms = head["pairs_s"], head["ms_per_step"] * K
+    step_ms = plain_steps if head["kind"] == "plain" else learned_steps
+    launches_per_step = plain_launches if head["kind"] == "plain" else learned_launches
+    accuracy = {"headline": head["config"], "epe_vs_plain_mm": head["epe_vs_plain_mm"], "epe_bar_mm": 1.0,
+                "epe_bar_met": bool(head["meets_epe_bar"]),
+                "epe_vs_ground_truth_mm": float(epe(plain_timed if head["kind"] == "plain" else learned, gt,
+                                                    valid).mean() * 1e3)}
+    learned_rec = {"pairs_s": learned_value, "iter_scale": scale, "energy_margin": margin,
+                   "fallbacks_per_step": fallbacks / K,
+                   "step_ms": [round(x, 3) for x in learned_steps],
+                   "epe_vs_plain_mm": float(ep_learned.mean() * 1e3),
+                   "epe_vs_plain_max_pair_mm": float(ep_learned.max() * 1e3),
+                   "meets_epe_bar": bool(ep_learned.mean() <= bar_m),
+                   "epe_vs_ground_truth_mm": {"learned": float(epe(learned, gt, valid).mean() * 1e3),
+                                              "plain": float(epe(plain_b, gt, valid).mean() * 1e3)},
+                   "energy_ratio_to_plain": float((e_learned / e_plain).mean()),
+                   "speedup_vs_plain_batched": learned_value / plain_value}
 
     # per-level phase times of one eager (ungraphed) plain solve of the batch:
     # set-up, iterations (with their algorithmic bandwidth) and median per level
@@ -477,13 +513,20 @@ def ours(args):
     opts = _lib.LearnedOpts(scale, margin)
     rep = _lib.LearnedReport()
 
+    def api_solve():
+        """The headline configuration's solve through the C ABI."""
+        if head["kind"] == "plain":
+            _lib.check(lib.pdflow_solve_batch(b.handle, B), "solve")
+        else:
+            _lib.check(lib.pdflow_solve_batch_learned(b.handle, B, net.handle, ctypes.byref(opts),
+                                                      ctypes.byref(rep)), "solve")
+
     def e2e_step():
         _lib.check(lib.pdflow_push_frames_u16(b.handle, B, ctypes.c_void_p(h[0].data_ptr()),
                                               ctypes.c_void_p(h[1].data_ptr())), "push")
         _lib.check(lib.pdflow_push_frames_u16(b.handle, B, ctypes.c_void_p(h[2].data_ptr()),
                                               ctypes.c_void_p(h[3].data_ptr())), "push")
-        _lib.check(lib.pdflow_solve_batch_learned(b.handle, B, net.handle, ctypes.byref(opts), ctypes.byref(rep)),
-                   "solve")
+        api_solve()
         _lib.check(lib.pdflow_read_flow_batch(b.handle, B, *[ctypes.c_void_p(x.data_ptr()) for x in hout]), "read")
 
     for _ in range(min(W, 2)):
@@ -526,8 +569,7 @@ def ours(args):
         b.push_raw_device(B, din[j][0].data_ptr(), din[j][1].data_ptr())
         b.push_raw_device(B, din[j][2].data_ptr(), din[j][3].data_ptr())
         ev["used"][j].record(stream)
-        _lib.check(lib.pdflow_solve_batch_learned(b.handle, B, net.handle, ctypes.byref(opts), ctypes.byref(rep)),
-                   "solve")
+        api_solve()
         _lib.check(lib.pdflow_copy_flow_device(b.handle, B, ctypes.c_void_p(dout[j][0].data_ptr()),
                                                ctypes.c_void_p(dout[j][1].data_ptr()),
                                                ctypes.c_void_p(dout[j][2].data_ptr())), "copy flow")
@@ -558,10 +600,13 @@ def ours(args):
         p1.record(copy)
     torch.cuda.synchronize()
     pipe_ms = p0.elapsed_time(p1)
+    e2e_check = b.read_flow(B)
     e2e = {"value": ws * B * ke / (pipe_ms / 1000.0), "unit": "pairs/s",
            "h2d_bytes_per_step": int(2 * B * WIDTH * HEIGHT * 3), "d2h_bytes_per_step": int(3 * B * N * 4),
+           "config": head["config"],
            "pipelined": "copies on a second stream overlap the neighbouring steps' solves",
-           "serial_value": e2e_serial}
+           "serial_value": e2e_serial,
+           "epe_vs_plain_mm": float(epe(e2e_check, plain_b, valid).mean() * 1e3)}
     b.close()
     net.close()
 

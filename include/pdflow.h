@@ -228,14 +228,19 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * synchronisations), one pixel per lane (form 2) or pixel pairs in packed
  * FP32x2 arithmetic (form 3: 40x40 tiles, 576 threads; form 4: 40x34 tiles,
  * 1008 threads; form 5: 24x24 tiles, 512 threads, two CTAs per SM; form 6:
- * 24x28 tiles, 288 threads owning two pairs each, two CTAs per SM).  pdflow_autotune times every eligible candidate of every
+ * 24x28 tiles, 288 threads owning two pairs each, two CTAs per SM; form 7:
+ * 24x24 tiles with the state in registers, 256 threads owning four rows each,
+ * two CTAs per SM, levels with rows % 4 == 0; form 8: the same regions
+ * walked by one persistent CTA per SM with the state and constants in
+ * registers while the next region streams into shared memory by TMA, levels
+ * with rows % 4 == 0).  pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The
  * handle's solution state is overwritten (the pushed frames are kept). */
-#define PDFLOW_TUNE_CANDIDATES 17     /* form 0, form 1, forms 2..6 x {2, 3, 4} iterations per launch */
+#define PDFLOW_TUNE_CANDIDATES 23     /* form 0, form 1, forms 2..8 x {2, 3, 4} iterations per launch */
 typedef struct pdflow_tune_level {
     int form;                         /* chosen form */
-    unsigned iters_per_launch;        /* chosen iterations per launch (forms 2..5) */
+    unsigned iters_per_launch;        /* chosen iterations per launch (forms 2..8) */
     float ms_per_iter[PDFLOW_TUNE_CANDIDATES];   /* per candidate; NaN if not eligible */
 } pdflow_tune_level;
 typedef struct pdflow_tune_report {
@@ -265,9 +270,11 @@ int pdflow_image_flow_device(pdflow_solver* s, const float** du, const float** d
  * For callers that cannot allocate device memory after start-up (a real-time
  * or safety-critical camera loop with a fixed memory budget, or a plugin whose
  * host framework owns every allocation): one pair solved entirely in scratch
- * memory compiled into this library, a 12 MiB __device__ array that every GPU
- * loading the library holds until the process exits.  It fits 320x240 frames
- * with rows <= 120; larger configurations return PDFLOW_ERR_ARG.
+ * memory compiled into this library, a 12 MiB __device__ array.  A GPU holds
+ * those 12 MiB from the first call on it (when the driver loads the array's
+ * module; with CUDA_MODULE_LOADING=EAGER from context creation) until the
+ * process exits.  It fits 320x240 frames with rows <= 120; larger
+ * configurations return PDFLOW_ERR_ARG.
  * Inputs: both frames as device pointers, row-major uint8 intensity and
  * uint16 depth (metres * 5000), height x width.  Outputs: device planes of
  * rows*cols floats (column-major, as pdflow_read_flow).  Work is queued on
@@ -276,7 +283,11 @@ int pdflow_image_flow_device(pdflow_solver* s, const float** du, const float** d
  * array's device address (cudaGetSymbolAddress) and sets kernel attributes:
  * make it before any stream capture.  All calls share the scratch array, which
  * keeps the last call's contents; calls that overlap on the GPU race on it and
- * must be serialised by the caller.  No cudaMalloc or cudaFree is called. */
+ * must be serialised by the caller.  No cudaMalloc or cudaFree is called.
+ * The kernels it runs (one-CTA launch at 15x20, scalar tiles above) contain
+ * no bounded device-side wait, so no device timeout can arise; launch errors
+ * are returned, and asynchronous execution errors surface at the caller's next
+ * synchronisation of `stream`. */
 int pdflow_solve_pair_noalloc(unsigned rows, unsigned width, unsigned height, const pdflow_params* params,
                               const uint8_t* d_intensity1, const uint16_t* d_depth1, const uint8_t* d_intensity2,
                               const uint16_t* d_depth2, float* d_dx, float* d_dy, float* d_dz, void* stream);

@@ -82,6 +82,12 @@ int pdflow_solve_levels(pdflow_solver* s, unsigned n, unsigned first, unsigned l
  * All modes give the same bits. */
 int pdflow_set_tile_copy_mode(int shape, int mode);
 
+/* Process-wide L2 prefetch distance of the register-resident quad tiles
+ * (iteration form 7), in CTAs: each CTA prefetches into L2 (one TMA tensor
+ * prefetch per plane) the region of the CTA that many launch positions later,
+ * which starts about when it finishes; 0 = no prefetch.  Same bits. */
+int pdflow_set_quad_prefetch(unsigned ctas_ahead);
+
 /* Per-level, per-phase timing of a plain solve of pairs [0, n) (tracing; no
  * counterpart in the reference, whose only timing is a host clock around the
  * whole solve): runs the solve eagerly (no graph) on the handle's stream with

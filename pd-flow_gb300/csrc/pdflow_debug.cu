@@ -134,7 +134,7 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 
 int pdflow_set_iteration_form(pdflow_solver* s, int form)
 {
-    if (!s || form < 0 || form > 6) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..6");
+    if (!s || form < 0 || form > 8) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..8");
     if (s->iter_form != form) {
         cudaStreamSynchronize(s->stream);
         s->iter_form = form;   // graphs are cached per iteration form
@@ -260,6 +260,13 @@ int pdflow_set_tile_copy_mode(int shape, int mode)
 {
     if (shape < 0 || shape > 3 || mode < 0 || mode > 7) return fail(PDFLOW_ERR_ARG, "shape 0..3, mode 0..7");
     set_tile_copy_mode(shape, mode);
+    return PDFLOW_OK;
+}
+
+int pdflow_set_quad_prefetch(unsigned ctas_ahead)
+{
+    if (ctas_ahead > (1u << 20)) return fail(PDFLOW_ERR_ARG, "prefetch distance above 2^20 CTAs");
+    set_quad_prefetch(ctas_ahead);
     return PDFLOW_OK;
 }
 

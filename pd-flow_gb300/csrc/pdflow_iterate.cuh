@@ -56,6 +56,25 @@ cudaError_t prepare_tiles2();
 cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
                                   unsigned kk, bool last, cudaStream_t st, int shape = 0,
                                   unsigned* status = nullptr);
+// Register-resident quad tiles (pdflow_quads.cu, iteration form 7): 32x32
+// regions, one thread per 4-row quad, constants by TMA (the step products
+// in L.qs, written by a kStepsQuads / kStepsAll set-up); same bits.  Needs
+// rows % 4 == 0 and 16-byte aligned planes (quads_eligible).
+cudaError_t prepare_quads();
+// Persistent streamed tiles (pdflow_ptiles.cu, iteration form 8): one CTA per
+// SM (`ctas` CTAs) walks every tile of the launch with its region in
+// registers while the next region streams into shared memory by TMA; same
+// preconditions (quads_eligible) and same bits.
+cudaError_t prepare_stream_tiles();
+size_t stream_smem_bytes();
+cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
+                                  unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas);
+// L2 prefetch distance of the quad tiles in CTAs (0 = off).
+void set_quad_prefetch(unsigned ctas_ahead);
+size_t quads_smem_bytes();
+bool quads_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst);
+cudaError_t launch_iterate_quads(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
+                                 unsigned kk, bool last, cudaStream_t st, unsigned* status);
 // Failure-detection probe: two CTAs where one waits (the grid form's bounded
 // neighbour wait, `polls` polls) for a progress counter the other never sets;
 // the wait runs out and records kStatusTimeout in *status.  flags: 2 counters.

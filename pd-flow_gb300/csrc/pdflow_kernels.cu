@@ -320,7 +320,7 @@ __global__ void k_im_gradients(LevelGeom g, PyrLevel n, LevelConsts L)
 // step sizes from mu, ri, rj, ddu, ddv in registers); the free spd plane then
 // holds powf(ddt, 2) for the level's median, so each pixel's square is taken
 // once instead of once per neighbour.
-__global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p, bool steps)
+__global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L, Params p, int steps)
 {
     const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
     o = at(o, po);
@@ -345,7 +345,7 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
     L.ddt[index] = ddt;
     L.ddu[index] = ddu;
     L.ddv[index] = ddv;
-    if (!steps) {
+    if (steps == kStepsNone) {
         L.mu[index] = data_weight(p.mu, ddu, ddv, ddt);
         L.spd[index] = powf(ddt, 2.f);
         return;
@@ -355,14 +355,29 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
     const float rj_m = (v > 0) ? L.rj[index - 1] : 0.f;
     const Steps s = mu_and_steps(p.mu, p.lambda_i, p.lambda_d, ddu, ddv, ddt, ri, rj, ri_m, rj_m, u > 0, v > 0);
     L.mu[index] = s.mu;
-    L.spd[index] = s.spd;
-    L.spuvx[index] = s.spuvx;
-    L.spuvy[index] = s.spuvy;
-    L.spwx[index] = s.spwx;
-    L.spwy[index] = s.spwy;
-    L.tu[index] = s.tu;
-    L.tv[index] = s.tv;
-    L.tw[index] = s.tw;
+    if (steps == kStepsRaw || steps == kStepsAll) {
+        L.spd[index] = s.spd;
+        L.spuvx[index] = s.spuvx;
+        L.spuvy[index] = s.spuvy;
+        L.spwx[index] = s.spwx;
+        L.spwy[index] = s.spwy;
+        L.tu[index] = s.tu;
+        L.tv[index] = s.tv;
+        L.tw[index] = s.tw;
+    } else {
+        L.spd[index] = powf(ddt, 2.f);   // the median's depth-change weight
+    }
+    if (steps == kStepsQuads || steps == kStepsAll) {
+        // the products the dual update forms (dual_update: mul(spd, mu), mul(spuvx, li), ...)
+        L.qs[0][index] = mul(s.spd, s.mu);
+        L.qs[1][index] = mul(s.spuvx, p.lambda_i);
+        L.qs[2][index] = mul(s.spuvy, p.lambda_i);
+        L.qs[3][index] = mul(s.spwx, p.lambda_d);
+        L.qs[4][index] = mul(s.spwy, p.lambda_d);
+        L.qs[5][index] = s.tu;
+        L.qs[6][index] = s.tv;
+        L.qs[7][index] = s.tw;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -724,7 +739,7 @@ cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cuda
 }
 
 cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p, cudaStream_t st,
-                              bool steps)
+                              int steps)
 {
     k_warp_steps<<<level_grid(g), kBlock, 0, st>>>(g, old_l, new_l, L, p, steps);
     return cudaGetLastError();

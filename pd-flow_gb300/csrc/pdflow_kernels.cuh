@@ -20,7 +20,20 @@ struct LevelConsts {
     float *dct, *dcu, *dcv, *ddt, *ddu, *ddv;
     float *mu, *du_prev, *dv_prev;
     float *spd, *spuvx, *spuvy, *spwx, *spwy, *tu, *tv, *tw;
+    // The step sizes as the iterations use them (levels run by the quad tiles):
+    // spd*mu, spuvx*lambda_i, spuvy*lambda_i, spwx*lambda_d, spwy*lambda_d, tu, tv, tw.
+    float* qs[8];
 };
+
+// Which step-size planes the warping kernel writes (launch_warp_steps).
+enum StepPlanes : int {
+    kStepsNone = 0,     // mu, and powf(ddt, 2) in spd for the median (tile levels that recompute their steps)
+    kStepsRaw = 1,      // mu and the eight raw step-size planes (spd .. tw)
+    kStepsQuads = 2,    // mu, powf(ddt, 2) in spd, and the eight iteration products in qs
+    kStepsAll = 3,      // mu, the raw planes and the products (every iteration form can run)
+};
+// Whether the median reads powf(ddt, 2) from spd after a set-up of this kind.
+inline bool steps_hold_ddt_sq(int mode) { return mode == kStepsNone || mode == kStepsQuads; }
 
 // Primal-dual state (planes of N floats).
 struct State {
@@ -84,6 +97,7 @@ __host__ __device__ __forceinline__ LevelConsts at(LevelConsts L, size_t o)
     r.mu = at(L.mu, o); r.du_prev = at(L.du_prev, o); r.dv_prev = at(L.dv_prev, o);
     r.spd = at(L.spd, o); r.spuvx = at(L.spuvx, o); r.spuvy = at(L.spuvy, o); r.spwx = at(L.spwx, o);
     r.spwy = at(L.spwy, o); r.tu = at(L.tu, o); r.tv = at(L.tv, o); r.tw = at(L.tw, o);
+    for (int k = 0; k < 8; ++k) r.qs[k] = at(L.qs[k], o);
     return r;
 }
 __host__ __device__ __forceinline__ State at(State S, size_t o)
@@ -132,9 +146,9 @@ cudaError_t launch_energy_prep(LevelGeom g, LevelSol sol, LevelConsts L, cudaStr
 cudaError_t launch_energy(LevelGeom g, LevelSol sol, LevelConsts L, Params p, float* energies, double* part,
                           cudaStream_t st);
 cudaError_t launch_im_gradients(LevelGeom g, PyrLevel new_l, LevelConsts L, cudaStream_t st);
-// steps = false writes mu but not the 8 step-size planes (levels run as tiles).
+// steps: which step-size planes to write (StepPlanes).
 cudaError_t launch_warp_steps(LevelGeom g, PyrLevel old_l, PyrLevel new_l, LevelConsts L, Params p,
-                              cudaStream_t st, bool steps = true);
+                              cudaStream_t st, int steps = kStepsRaw);
 cudaError_t launch_dual(LevelGeom g, LevelConsts L, State S, Params p, cudaStream_t st);
 cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old,
                           cudaStream_t st);

@@ -9,9 +9,11 @@
 // not change between frames.  The regular entry points (pdflow_create and
 // friends) allocate one arena per handle; this one allocates nothing.
 //
-// The scratch is a file-scope __device__ array of kScratchBytes (12 MiB), so
-// every GPU that loads this library holds those 12 MiB until the process
-// exits, whether or not the entry point is ever called.  It fits 320x240
+// The scratch is a file-scope __device__ array of kScratchBytes (12 MiB).  This
+// translation unit has no kernels, so under CUDA's default lazy module loading
+// its module (and with it the array) is loaded on a device by the first call's
+// cudaGetSymbolAddress; from then (with CUDA_MODULE_LOADING=EAGER, from context
+// creation) the GPU holds the 12 MiB until the process exits.  It fits 320x240
 // frames with rows <= 120 (about 8.8 MB of pyramid and level buffers);
 // larger configurations are rejected with PDFLOW_ERR_ARG.
 //
@@ -140,6 +142,10 @@ int pdflow_solve_pair_noalloc(unsigned rows, unsigned width, unsigned height, co
     if (params) s.prm = *params;
     else pdflow_default_params(rows, &s.prm);
     s.use_graph = 0;
+    // Scalar tiles (form 2): they need no per-launch tensor maps and contain no
+    // bounded wait, so nothing here can time out on the device; the paired
+    // forms give the same bits (the tests compare against the regular entry
+    // point, whose default is the paired 24x24 form).
     s.iter_form = 2;
     size_t need = 0;
     pdflow::carve_solver(&s, nullptr, &need);

@@ -1,0 +1,379 @@
+// Persistent, register-resident tile iterations ("streamed tiles", iteration
+// form 8).
+//
+// One CTA per SM walks a list of tiles (every 24 x 24 interior of every pair
+// of the launch, 4-pixel halo: 32 x 32 regions, as in pdflow_tiles2.cu).  A
+// tile's 13 state planes and 19 level constants (11 set-up planes and the 8
+// step products) live in registers while its kk <= 4 iterations run: each of
+// the 512 threads owns a vertical pixel pair (rows 2p, 2p+1 of region column
+// c) and computes it with packed FP32x2 instructions.  Meanwhile the TMA unit
+// copies the next tile's 32 planes into a shared-memory staging buffer (one
+// tensor copy per plane, completing on an mbarrier), so the region loads run
+// behind the arithmetic instead of between launches' compute phases.
+//
+// Neighbours: the row below the pair (dual step) and above it (primal step)
+// by warp shuffles inside the column's 16 lanes; the column to the right
+// (dual) and to the left (primal) through six shared exchange planes, into
+// which each thread publishes what its neighbours read (U = du_acc + du_prev,
+// V = dv_acc + dv_prev, W = dw_acc; ri * the u-component of each TV dual).
+// These are the same rounded expressions the reference evaluates
+// (computeGradient, computeDivergence: pdflow_cudalib.cu:935-1013), so the
+// results are bit-identical to every other iteration form.  Every pixel of
+// the region is updated in every iteration; the stale ring at non-border
+// region edges is never read by an exact pixel and only the interior is
+// stored.  Needs rows % 4 == 0 (16-byte aligned tensor-copy rows).
+#include <cuda.h>
+
+#include "pdflow_iterate.cuh"
+#include "pdflow_math.cuh"
+#include "pdflow_pack.cuh"
+
+namespace pdflow {
+
+namespace {
+
+using namespace pack;
+
+constexpr int kSH = 4;                         // halo (iterations per launch at most)
+constexpr int kST = 24;                        // interior rows and columns
+constexpr int kSR = kST + 2 * kSH;             // region rows and columns (32)
+constexpr int kSPlane = kSR * kSR;             // floats per shared plane
+constexpr int kSThreads = kSR * kSR / 2;       // one thread per pixel pair (512)
+
+// staging planes (TMA destinations, in this order): 13 state, 19 constants;
+// then the six exchange planes
+enum { S_DU, S_DV, S_DW, S_UA, S_VA, S_WA, S_PD, S_PUU, S_PUV, S_PVU, S_PVV, S_PWU, S_PWV,
+       K_DUP, K_DVP, K_RI, K_RJ, K_DDT, K_DDU, K_DDV, K_S0, K_S1, K_S2, K_S3, K_S4,
+       K_MU, K_DCT, K_DCU, K_DCV, K_TU, K_TV, K_TW,
+       N_STAGE,
+       X_U = N_STAGE, X_V, X_W, Y_U, Y_V, Y_W, N_PLANES };
+
+struct StreamArgs {
+    LevelGeom g;
+    float* dst[13];            // du dv dw du_acc dv_acc dw_acc pd puu puv pvu pvv pwu pwv (interior written)
+    const float* depth_old;
+    Params p;
+    unsigned kk;
+    bool last;
+    unsigned tiles_v;          // tiles per column of tiles
+    unsigned tiles;            // tiles per pair
+    unsigned total;            // tiles of the launch (tiles * pairs)
+    unsigned* status;          // device word: kStreamTimeout when a bounded wait gives up
+};
+
+// 3D maps (rows, columns, arena slots) of the 13 source state planes and the
+// 19 constant planes, box = one region.
+struct StreamMaps {
+    CUtensorMap m[N_STAGE];
+};
+
+constexpr unsigned kStreamTimeout = 0x5354524Du;
+constexpr uint32_t kStreamWaitLimit = 1u << 22;
+
+__device__ __forceinline__ float clamp1(float pd) { return (fabsf(pd) > 1.f) ? ((pd > 1.f) ? 1.f : -1.f) : pd; }
+
+__device__ __forceinline__ void disc(float& a, float& b)
+{
+    const float m = rhypotf(a, b);
+    if (m < 1.f) {
+        a = mul(a, m);
+        b = mul(b, m);
+    }
+}
+
+// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).
+__device__ __forceinline__ void shrink(float& du, float& dv, float of, float th, float a1, float b1)
+{
+    if (of < -th) {
+        du = add(du, a1);
+        dv = add(dv, b1);
+    } else if (of > th) {
+        du = sub(du, a1);
+        dv = sub(dv, b1);
+    } else {
+        const float den = add(th, 1e-10f);
+        du = sub(du, qt(mul(a1, of), den));
+        dv = sub(dv, qt(mul(b1, of), den));
+    }
+}
+
+struct Tile {
+    unsigned y;                // grid pair index
+    int rv0, ru0, iv0, iv1, iu0, iu1;
+};
+
+__device__ __forceinline__ Tile tile_at(const StreamArgs& a, unsigned n)
+{
+    Tile t;
+    t.y = n / a.tiles;
+    const unsigned x = n % a.tiles;
+    const int R = (int)a.g.R, C = (int)a.g.C;
+    const int tv = (int)(x % a.tiles_v), tu = (int)(x / a.tiles_v);
+    t.iv0 = tv * kST;
+    t.iu0 = tu * kST;
+    t.iv1 = min(t.iv0 + kST, R);
+    t.iu1 = min(t.iu0 + kST, C);
+    t.rv0 = max(t.iv0 - kSH, 0);
+    t.ru0 = max(t.iu0 - kSH, 0);
+    return t;
+}
+
+// Thread 0: the tensor copies of tile n's region into the staging planes,
+// completing on `bar` (the caller's threads have finished reading staging).
+__device__ __forceinline__ void issue_region(const StreamArgs& a, const StreamMaps& tm, float* sm, uint32_t bar,
+                                             unsigned n)
+{
+    const Tile t = tile_at(a, n);
+    const int slot = (int)(a.g.map ? (__ldg(a.g.map + t.y) & kMapSlotMask) : t.y);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // earlier generic reads before async writes
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"((uint32_t)N_STAGE * (uint32_t)kSPlane * 4u)
+                 : "memory");
+#pragma unroll
+    for (int k = 0; k < N_STAGE; ++k)
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(sm + k * kSPlane)),
+            "l"(reinterpret_cast<uint64_t>(&tm.m[k])), "r"(t.rv0), "r"(t.ru0), "r"(slot), "r"(bar)
+            : "memory");
+}
+
+__global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, const __grid_constant__ StreamMaps tm)
+{
+    extern __shared__ __align__(128) float sm[];
+    __shared__ __align__(8) unsigned long long bar_mem;
+    const int t = threadIdx.x;
+    const int c = t >> 4, p = t & 15;              // region column, pixel pair
+    const int me = c * kSR + 2 * p;                 // the pair's offset in a shared plane
+    const int right = (c + 1 < kSR ? c + 1 : c) * kSR + 2 * p;   // beyond the region: own storage
+    const int left = (c > 0 ? c - 1 : c) * kSR + 2 * p;
+    const uint32_t bar = smem_u32(&bar_mem);
+    const int R = (int)a.g.R, C = (int)a.g.C;
+    const float li = a.p.lambda_i, ld = a.p.lambda_d;
+    const float2 li2 = make_float2(li, li), ld2 = make_float2(ld, ld), two = make_float2(2.f, 2.f);
+    const float2 zero = make_float2(0.f, 0.f);
+    float* XU = sm + X_U * kSPlane;
+    float* XV = sm + X_V * kSPlane;
+    float* XW = sm + X_W * kSPlane;
+    float* YU = sm + Y_U * kSPlane;
+    float* YV = sm + Y_V * kSPlane;
+    float* YW = sm + Y_W * kSPlane;
+    auto ld2s = [&](int plane) { return *reinterpret_cast<const float2*>(sm + plane * kSPlane + me); };
+
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (blockIdx.x < a.total) issue_region(a, tm, sm, bar, blockIdx.x);
+    }
+    __syncthreads();   // the mbarrier's initialisation before anyone waits on it
+    uint32_t phase = 0;
+    for (unsigned n = blockIdx.x; n < a.total; n += gridDim.x) {
+        const Tile tl = tile_at(a, n);
+        const size_t po = pair_off(a.g.map, a.g.pstride, tl.y);
+        const int u = tl.ru0 + c, v0 = tl.rv0 + 2 * p;
+        const bool live = u < C && v0 < R;           // v0 < R implies v0 + 1 < R (R even)
+        const bool fu = (u == 0), lu = (u == C - 1);
+        const bool fv = (v0 == 0), lv = (v0 + 1 == R - 1);
+        const bool last_launch = a.last || (pair_flags(a.g.map, tl.y) & kMapLast);
+
+        const bool ok = mbar_wait(bar, phase, kStreamWaitLimit);
+        float2 du = ld2s(S_DU), dv = ld2s(S_DV), dw = ld2s(S_DW), ua = ld2s(S_UA), va = ld2s(S_VA),
+               wa = ld2s(S_WA), pd = ld2s(S_PD), puu = ld2s(S_PUU), puv = ld2s(S_PUV), pvu = ld2s(S_PVU),
+               pvv = ld2s(S_PVV), pwu = ld2s(S_PWU), pwv = ld2s(S_PWV);
+        const float2 dup = ld2s(K_DUP), dvp = ld2s(K_DVP), ri = ld2s(K_RI), rj = ld2s(K_RJ), ddt = ld2s(K_DDT),
+                     ddu = ld2s(K_DDU), ddv = ld2s(K_DDV), s0 = ld2s(K_S0), s1 = ld2s(K_S1), s2 = ld2s(K_S2),
+                     s3 = ld2s(K_S3), s4 = ld2s(K_S4), mu = ld2s(K_MU), dct = ld2s(K_DCT), dcu = ld2s(K_DCU),
+                     dcv = ld2s(K_DCV), tu = ld2s(K_TU), tv = ld2s(K_TV), tw = ld2s(K_TW);
+        // staging read by every thread: the next region may land.  A wait that ran
+        // out anywhere ends the whole CTA (values read above are then unused)
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) {
+                if (a.status) atomicExch(a.status, kStreamTimeout);
+                mbar_wait(bar, phase, kStreamWaitLimit);   // bounded: the copies still in flight
+            }
+            return;
+        }
+        phase ^= 1u;
+        if (t == 0 && n + gridDim.x < a.total) issue_region(a, tm, sm, bar, n + gridDim.x);
+
+        const float2 mudu = mul2(mu, ddu), mudv = mul2(mu, ddv);
+        const float2 a1 = mul2(tu, dcu), b1 = mul2(tv, dcv);
+        const float2 th = fm2(a1, dcu, mul2(b1, dcv));
+        for (unsigned j = 0; j < a.kk; ++j) {
+            // ---------------- dual step (computeGradient + updateDualVariables) ----------------
+            {
+                const float2 U = add2(ua, dup), V = add2(va, dvp);
+                *reinterpret_cast<float2*>(XU + me) = U;
+                *reinterpret_cast<float2*>(XV + me) = V;
+                *reinterpret_cast<float2*>(XW + me) = wa;
+                const float Ub = __shfl_down_sync(0xffffffffu, U.x, 1, 16);   // the next pair's first row
+                const float Vb = __shfl_down_sync(0xffffffffu, V.x, 1, 16);
+                const float Wb = __shfl_down_sync(0xffffffffu, wa.x, 1, 16);
+                __syncthreads();
+                float2 gu1 = zero, gv1 = zero, gw1 = zero;
+                if (!lu) {
+                    gu1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XU + right), U));
+                    gv1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XV + right), V));
+                    gw1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XW + right), wa));
+                }
+                float2 gu2 = mul2(rj, sub2(make_float2(U.y, Ub), U));
+                float2 gv2 = mul2(rj, sub2(make_float2(V.y, Vb), V));
+                float2 gw2 = mul2(rj, sub2(make_float2(wa.y, Wb), wa));
+                if (lv) {
+                    gu2.y = 0.f;
+                    gv2.y = 0.f;
+                    gw2.y = 0.f;
+                }
+                const float2 X = fm2(ddv, va, fm2(ddu, ua, sub2(ddt, wa)));
+                pd = fm2(s0, X, pd);
+                puu = fm2(s1, gu1, puu);
+                puv = fm2(s2, gu2, puv);
+                pvu = fm2(s1, gv1, pvu);
+                pvv = fm2(s2, gv2, pvv);
+                pwu = fm2(s3, gw1, pwu);
+                pwv = fm2(s4, gw2, pwv);
+                pd.x = clamp1(pd.x);
+                pd.y = clamp1(pd.y);
+                disc(puu.x, puv.x);
+                disc(puu.y, puv.y);
+                disc(pvu.x, pvv.x);
+                disc(pvu.y, pvv.y);
+                disc(pwu.x, pwv.x);
+                disc(pwu.y, pwv.y);
+            }
+            // ---------------- primal step (computeDivergence + updatePrimalVariables) ----------------
+            {
+                const float2 yu = mul2(ri, puu), yv = mul2(ri, pvu), yw = mul2(ri, pwu);
+                *reinterpret_cast<float2*>(YU + me) = yu;
+                *reinterpret_cast<float2*>(YV + me) = yv;
+                *reinterpret_cast<float2*>(YW + me) = yw;
+                const float2 zu = mul2(rj, puv), zv = mul2(rj, pvv), zw = mul2(rj, pwv);
+                const float zua = __shfl_up_sync(0xffffffffu, zu.y, 1, 16);   // the previous pair's second row
+                const float zva = __shfl_up_sync(0xffffffffu, zv.y, 1, 16);
+                const float zwa = __shfl_up_sync(0xffffffffu, zw.y, 1, 16);
+                __syncthreads();
+                const float2 pu_[3] = {puu, pvu, pwu}, pv_[3] = {puv, pvv, pwv};
+                const float2 zm_[3] = {make_float2(zua, zu.x), make_float2(zva, zv.x), make_float2(zwa, zw.x)};
+                const float* Yp[3] = {YU, YV, YW};
+                float2 div[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float2 d;
+                    if (fu) d = mul2(ri, pu_[k]);
+                    else if (lu) d = neg2(*reinterpret_cast<const float2*>(Yp[k] + left));
+                    else d = fm2(ri, pu_[k], neg2(*reinterpret_cast<const float2*>(Yp[k] + left)));
+                    float2 g = add2(d, fm2(rj, pv_[k], neg2(zm_[k])));
+                    if (fv) g.x = fm(rj.x, pv_[k].x, d.x);
+                    if (lv) g.y = fm(-rj.x, pv_[k].x, d.y);
+                    div[k] = g;
+                }
+                const float2 du_old = du, dv_old = dv, dw_old = dw;
+                du = fm2(neg2(tu), fm2(mudu, pd, neg2(mul2(li2, div[0]))), du);
+                dv = fm2(neg2(tv), fm2(mudv, pd, neg2(mul2(li2, div[1]))), dv);
+                {
+                    // per lane: see pdflow_pack.cuh on contraction of packed products
+                    const float2 tq = fm2(neg2(mu), pd, neg2(mul2(ld2, div[2])));
+                    dw.x = add(dw.x, mul(-tw.x, tq.x));
+                    dw.y = add(dw.y, mul(-tw.y, tq.y));
+                }
+                const float2 of = fm2(dcv, dv, fm2(dcu, du, dct));
+                shrink(du.x, dv.x, of.x, th.x, a1.x, b1.x);
+                shrink(du.y, dv.y, of.y, th.y, a1.y, b1.y);
+                ua = fm2(two, du, neg2(du_old));
+                va = fm2(two, dv, neg2(dv_old));
+                wa = fm2(two, dw, neg2(dw_old));
+                if (last_launch && j + 1 == a.kk && live) {
+                    // saturateVariables (pdflow_cudalib.cu:1018-1038) after the level's last iteration
+                    const float2 z = __ldg(reinterpret_cast<const float2*>(at(a.depth_old, po) + v0 +
+                                                                            (size_t)u * (size_t)R));
+                    saturate(du.x, dv.x, dw.x, dup.x, dvp.x, z.x);
+                    saturate(du.y, dv.y, dw.y, dup.y, dvp.y, z.y);
+                }
+            }
+            // no barrier here: this iteration's exchange reads happen before the next
+            // one's first barrier, and the next stores to the same planes after it
+        }
+
+        // ---- the interior to the destination buffer ----
+        if (live && v0 >= tl.iv0 && v0 < tl.iv1 && u >= tl.iu0 && u < tl.iu1) {
+            const size_t gi = (size_t)v0 + (size_t)u * (size_t)R;
+            const float2 st[13] = {du, dv, dw, ua, va, wa, pd, puu, puv, pvu, pvv, pwu, pwv};
+#pragma unroll
+            for (int k = 0; k < 13; ++k) *reinterpret_cast<float2*>(at(a.dst[k], po) + gi) = st[k];
+        }
+        // the next tile's staging wait is followed by a barrier before its first
+        // exchange store, so the exchange planes need none here
+    }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn stream_encoder()
+{
+    static const EncodeTiledFn fn = [] {
+        void* q = nullptr;
+        cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &q, 12000, cudaEnableDefault, &qr) !=
+                cudaSuccess ||
+            qr != cudaDriverEntryPointSuccess)
+            q = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(q);
+    }();
+    return fn;
+}
+
+}  // namespace
+
+size_t stream_smem_bytes() { return sizeof(float) * N_PLANES * kSPlane; }
+
+cudaError_t prepare_stream_tiles()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_iterate_stream, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)stream_smem_bytes());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_iterate_stream, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    return e;
+}
+
+cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
+                                  unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas)
+{
+    // same preconditions as the quad tiles (16-byte aligned planes, rows % 4 == 0)
+    if (kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0 || !stream_encoder())
+        return cudaErrorInvalidValue;
+    StreamArgs a;
+    a.g = g;
+    float* d13[13] = {dst.du, dst.dv, dst.dw, dst.dua, dst.dva, dst.dwa, dst.pd,
+                      dst.puu, dst.puv, dst.pvu, dst.pvv, dst.pwu, dst.pwv};
+    for (int k = 0; k < 13; ++k) a.dst[k] = d13[k];
+    a.depth_old = depth_old;
+    a.p = p;
+    a.kk = kk;
+    a.last = last;
+    a.status = status;
+    a.tiles_v = (g.R + kST - 1) / kST;
+    a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
+    a.total = a.tiles * g.pairs;
+    StreamMaps maps{};
+    const float* planes[N_STAGE] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,
+                                    src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv,
+                                    L.du_prev, L.dv_prev, L.ri, L.rj, L.ddt, L.ddu, L.ddv,
+                                    L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4],
+                                    L.mu, L.dct, L.dcu, L.dcv, L.qs[5], L.qs[6], L.qs[7]};
+    const cuuint64_t dims[3] = {g.R, g.C, g.slots};
+    const cuuint64_t strides[2] = {cuuint64_t(g.R) * 4u, g.pstride};
+    const cuuint32_t box[3] = {kSR, kSR, 1}, estr[3] = {1, 1, 1};
+    const EncodeTiledFn encode = stream_encoder();
+    for (int k = 0; k < N_STAGE; ++k)
+        if (encode(&maps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(planes[k]), dims, strides, box,
+                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    const unsigned grid = ctas < a.total ? ctas : a.total;
+    k_iterate_stream<<<grid, kSThreads, stream_smem_bytes(), st>>>(a, maps);
+    return cudaGetLastError();
+}
+
+}  // namespace pdflow

@@ -117,6 +117,7 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
                     &L.dcu, &L.dcv, &L.ddt, &L.ddu, &L.ddv, &L.mu, &L.du_prev, &L.dv_prev, &L.spd, &L.spuvx,
                     &L.spuvy, &L.spwx, &L.spwy, &L.tu, &L.tv, &L.tw};
     for (float** p : lp) *p = cv.plane(N);
+    for (float*& p : L.qs) p = cv.plane(N);
     State& S = s->S;
     float** sp[] = {&S.du, &S.dv, &S.dw, &S.dua, &S.dva, &S.dwa, &S.pd, &S.puu, &S.puv, &S.pvu, &S.pvv, &S.pwu,
                     &S.pwv};
@@ -195,6 +196,28 @@ static bool level_runs_tiles(const pdflow_solver* s, const LevelGeom& g, unsigne
     return s->iter_form >= 2 && iters > 0 && (pairs > 1 || g.N > 300u);
 }
 
+// Whether level `level`'s tiles run register-resident (quad tiles, form 7, or
+// streamed tiles, form 8): chosen for the level and possible at its size
+// (rows % 4 == 0; other levels of such a solve run the paired 24x24 tiles,
+// form 5).
+static bool level_runs_quads(const pdflow_solver* s, const LevelGeom& g, unsigned iters, unsigned pairs,
+                             unsigned level)
+{
+    if (!level_runs_tiles(s, g, iters, pairs, level)) return false;
+    const int forced = level < 8 ? s->level_form[level] : -1;
+    const int form = forced >= 0 ? forced : s->iter_form;
+    return (form == 7 || form == 8) && quads_eligible(g, s->L, s->S, s->S);
+}
+
+// The step-size planes the level's set-up writes for its iteration form.
+static int level_steps(const pdflow_solver* s, const LevelGeom& g, unsigned iters, unsigned pairs, unsigned level,
+                       bool all_steps)
+{
+    if (all_steps) return kStepsAll;
+    if (!level_runs_tiles(s, g, iters, pairs, level)) return kStepsRaw;
+    return level_runs_quads(s, g, iters, pairs, level) ? kStepsQuads : kStepsNone;
+}
+
 // Enqueues `iters` iterations of level i for pairs [0, pairs) in the
 // solve's launch form; returns the number of kernels launched via *count.
 // The final duals' buffer is reported in *fin.
@@ -210,8 +233,9 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
     const int form = forced >= 0 ? forced : s->iter_form;
     const bool one_launch = forced >= 0 ? (forced == 1 && iters > 0 && one_launch_ok)
                                         : (s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok);
+    const bool quads = tiles && level_runs_quads(s, g, iters, pairs, level);
     const bool paired = tiles && form >= 3;
-    const int shape = form - 3;   // 40x40, 40x34, 24x24 or 24x28 tiles
+    const int shape = form >= 7 ? 2 : form - 3;   // 40x40, 40x34, 24x24 or 24x28 tiles (forms 7, 8 elsewhere: 24x24)
     if (tiles) {
         State cur = s->S;
         State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
@@ -221,7 +245,14 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
                                : tiles_halo();
         for (unsigned done = 0; done < iters;) {
             const unsigned kk = (iters - done < h) ? iters - done : h;
-            if (paired)
+            if (quads && form == 8)
+                CUDA_TRY(launch_iterate_stream(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, s->status,
+                                               unsigned(s->num_sms)),
+                         "streamed tile iteration launch");
+            else if (quads)
+                CUDA_TRY(launch_iterate_quads(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, s->status),
+                         "quad tile iteration launch");
+            else if (paired)
                 CUDA_TRY(launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, shape,
                                                s->status),
                          "tile iteration launch");
@@ -321,7 +352,7 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
         if (tr) CUDA_TRY(cudaEventRecord(tr[0], st), "trace event");
         CUDA_TRY(launch_level_init(g, i == 0, s->sol, o, n, s->L, s->S, st, seed), "level init launch");
         const unsigned iters = scaled_iters(s->prm.num_max_iter[i], plan.iter_scale);
-        const bool steps = plan.all_steps || !level_runs_tiles(s, g, iters, pairs, i);
+        const int steps = level_steps(s, g, iters, pairs, i, plan.all_steps);
         CUDA_TRY(launch_im_gradients(g, n, s->L, st), "image gradients launch");
         CUDA_TRY(launch_warp_steps(g, o, n, s->L, p, st, steps), "warping launch");
         count += 3;
@@ -335,7 +366,7 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
         }
         if (tr) CUDA_TRY(cudaEventRecord(tr[2], st), "trace event");
         CUDA_TRY(launch_median(g, i + 1 == s->ctf_levels, o, s->L, fin, s->sol, s->dx, s->dy, s->dz, p, nullptr, st,
-                               nullptr, !steps),
+                               nullptr, steps_hold_ddt_sq(steps)),
                  "median launch");
         ++count;
         if (int(i) == plan.energy_level && plan.energy) {
@@ -472,6 +503,8 @@ int pdflow_create_batch(unsigned rows, unsigned width, unsigned height, const pd
             CUDA_TRY(prepare_iterate(), "kernel attributes");
             CUDA_TRY(prepare_tiles(), "kernel attributes");
             CUDA_TRY(prepare_tiles2(), "kernel attributes");
+            CUDA_TRY(prepare_quads(), "kernel attributes");
+            CUDA_TRY(prepare_stream_tiles(), "kernel attributes");
             if (dev < 64) prepared |= 1ull << dev;
         }
     }

@@ -17,9 +17,10 @@ struct Candidate {
     int form;
     unsigned kk;
 };
-constexpr Candidate kCandidates[PDFLOW_TUNE_CANDIDATES] = {{0, 0}, {1, 0}, {2, 2}, {2, 3}, {2, 4}, {3, 2},
-                                                            {3, 3}, {3, 4}, {4, 2}, {4, 3}, {4, 4}, {5, 2},
-                                                            {5, 3}, {5, 4}, {6, 2}, {6, 3}, {6, 4}};
+constexpr Candidate kCandidates[PDFLOW_TUNE_CANDIDATES] = {{0, 0}, {1, 0}, {2, 2}, {2, 3}, {2, 4}, {3, 2}, {3, 3},
+                                                            {3, 4}, {4, 2}, {4, 3}, {4, 4}, {5, 2}, {5, 3}, {5, 4},
+                                                            {6, 2}, {6, 3}, {6, 4}, {7, 2}, {7, 3}, {7, 4},
+                                                            {8, 2}, {8, 3}, {8, 4}};
 
 void drop_graphs(pdflow_solver* s)
 {
@@ -35,8 +36,8 @@ extern "C" {
 
 int pdflow_set_level_form(pdflow_solver* s, unsigned level, int form, unsigned iters_per_launch)
 {
-    if (!s || level >= 8 || form < -1 || form > 6 || iters_per_launch > 4) {
-        set_last_error("bad argument (form -1..6, level < 8, iterations per launch 0..4)");
+    if (!s || level >= 8 || form < -1 || form > 8 || iters_per_launch > 4) {
+        set_last_error("bad argument (form -1..8, level < 8, iterations per launch 0..4)");
         return PDFLOW_ERR_ARG;
     }
     drop_graphs(s);
@@ -84,6 +85,7 @@ int pdflow_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_t
         for (int c = 0; c < PDFLOW_TUNE_CANDIDATES; ++c) {
             rep.level[i].ms_per_iter[c] = NAN;
             if (kCandidates[c].form == 1 && !one_ok) continue;
+            if (kCandidates[c].form >= 7 && !quads_eligible(g, s->L, s->S, s->S)) continue;   // rows % 4 != 0
             s->level_form[i] = kCandidates[c].form;
             s->level_kk[i] = kCandidates[c].kk;
             float t = INFINITY;

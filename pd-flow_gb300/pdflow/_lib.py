@@ -32,7 +32,7 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
-TUNE_CANDIDATES = 17   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..6 x {2, 3, 4} iterations per launch
+TUNE_CANDIDATES = 23   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..8 x {2, 3, 4} iterations per launch
 
 
 class TuneLevel(ctypes.Structure):
@@ -179,6 +179,7 @@ _SIGNATURES = {
     "pdflow_autotune": (ctypes.c_int, [vp, u32, u32, ctypes.POINTER(TuneReport)]),
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "pdflow_set_quad_prefetch": (ctypes.c_int, [ctypes.c_uint]),
     "pdflow_debug_wait_timeout": (ctypes.c_int, [vp, u32]),
     "pdflow_trace_solve": (ctypes.c_int, [vp, u32, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),

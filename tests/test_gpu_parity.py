@@ -48,11 +48,15 @@ CASES = [("qvga_s0.npz", 240, 320, 240), ("qvga_s0.npz", 60, 320, 240),
          ("vga_s2.npz", 480, 640, 480), ("vga_s2.npz", 240, 640, 480)]
 
 
+@pytest.mark.parametrize("form", [1, 7, 8])
 @pytest.mark.parametrize("fixture,rows,w,h", CASES)
-def test_flow_matches_reference_cuda_path(fixture, rows, w, h):
+def test_flow_matches_reference_cuda_path(fixture, rows, w, h, form):
+    """The final flow equals the reference's own CUDA build bit for bit, with
+    the level iterations as one persistent launch (form 1) or as register-
+    resident quad tiles (form 7)."""
     from conftest import load_golden
     g = load_golden(fixture)
-    out = solve(g, rows, w, h)
+    out = solve(g, rows, w, h, form=form)
     for c, o in zip(("dx", "dy", "dz"), out):
         ref = g[f"r{rows}_{c}"]
         d = np.abs(o.astype(np.float64) - ref)
@@ -192,12 +196,13 @@ def test_graph_and_stream_forms_agree(golden_qvga):
 
 @pytest.mark.parametrize("fixture,rows,w,h", [CASES[0], CASES[2]])
 def test_iteration_forms_agree(fixture, rows, w, h):
-    """Temporally blocked tiles, one launch per level's iterations
-    (slab-persistent kernel) and two kernels per iteration give the same bits."""
+    """Temporally blocked tiles (scalar, paired, register-resident quads),
+    one launch per level's iterations (slab-persistent kernel) and two kernels
+    per iteration give the same bits."""
     from conftest import load_golden
     g = load_golden(fixture)
     a = solve(g, rows, w, h, form=2)
-    for form in (1, 0):
+    for form in (1, 0, 5, 7, 8):
         b = solve(g, rows, w, h, form=form)
         for x, y in zip(a, b):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), form

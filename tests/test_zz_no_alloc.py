@@ -34,18 +34,28 @@ def regular(rows, frames):
     return out
 
 
-def noalloc(lib, torch, rows, frames):
+def device_buffers(torch, rows, frames):
+    """The caller's own device buffers: both frames and the three flow planes."""
     i1, z1, i2, z2 = frames
-    h, w = i1.shape
     cols = rows * 320 // 240
     dev = [torch.from_numpy(np.ascontiguousarray(a.view(np.int16) if a.dtype == np.uint16 else a)).cuda()
            for a in (i1, z1, i2, z2)]
     out = [torch.full((rows * cols,), float("nan"), dtype=torch.float32, device="cuda") for _ in range(3)]
+    return dev, out
+
+
+def call_noalloc(lib, torch, rows, frames, dev, out):
+    h, w = frames[0].shape
     stream = torch.cuda.current_stream()
     rc = lib.pdflow_solve_pair_noalloc(rows, w, h, None, *[ctypes.c_void_p(t.data_ptr()) for t in dev + out],
                                        ctypes.c_void_p(stream.cuda_stream))
     assert rc == 0, lib.pdflow_last_error()
     torch.cuda.synchronize()
+
+
+def noalloc(lib, torch, rows, frames):
+    dev, out = device_buffers(torch, rows, frames)
+    call_noalloc(lib, torch, rows, frames, dev, out)
     return [t.cpu().numpy() for t in out]
 
 
@@ -78,3 +88,23 @@ def test_noalloc_rejects_configurations_beyond_its_scratch(built_lib):
                                              p(out.data_ptr()), p(out.data_ptr()), None)
     assert rc == ERR_ARG
     assert b"scratch" in built_lib.pdflow_last_error()
+
+
+def test_noalloc_calls_after_the_first_allocate_no_device_memory(built_lib):
+    """The property the entry point exists for: once the first call on the
+    device has loaded the scratch array, further calls change neither the
+    device's free memory (cudaMemGetInfo) nor torch's allocator statistics."""
+    torch = pytest.importorskip("torch")
+    frames = [scenes.make_pair(33 + k, vga=False, n_objects=3) for k in range(2)]
+    bufs = [device_buffers(torch, 120, f) for f in frames]
+    call_noalloc(built_lib, torch, 120, frames[0], *bufs[0])   # first call: one-time set-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for f, b in zip(frames, bufs):
+        call_noalloc(built_lib, torch, 120, f, *b)
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0
+    for key in ("allocation.all.allocated", "reserved_bytes.all.current", "allocated_bytes.all.current"):
+        assert stats1.get(key, 0) == stats0.get(key, 0), key
