@@ -70,6 +70,51 @@ def dist_env():
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def free_port() -> int:
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def spawn_replicas(n: int, argv) -> int:
+    """`--gpus N` without torchrun: start N copies of this script with the
+    environment torchrun would give them (RANK, LOCAL_RANK, WORLD_SIZE and a
+    127.0.0.1 rendezvous), one per GPU.  Rank 0's stdout is this process's
+    (it prints the one JSON line); the others print nothing.  Returns the
+    worst exit code."""
+    port = free_port()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, WORLD_SIZE=str(n), RANK=str(r), LOCAL_RANK=str(r), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *argv], env=env,
+                                      stdout=None if r == 0 else subprocess.DEVNULL))
+    codes = [p.wait() for p in procs]
+    return max(codes, key=abs)
+
+
+def replica_selftest(args) -> int:
+    """Host-side check of the replica path (no GPU): every rank reports a
+    synthetic elapsed time of 100 ms x (rank + 1) for `--batch` pairs x
+    `--steps` steps over gloo, and rank 0 prints the job line that
+    replica_value makes of them."""
+    import torch
+    import torch.distributed as dist
+    ws, rank, _ = dist_env()
+    if ws > 1:
+        dist.init_process_group("gloo")
+    value, slowest = replica_value(torch, 100.0 * (rank + 1), args.batch, args.steps)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+                          "ms_per_step": slowest / args.steps, "selftest": True}), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def make_workload(n_distinct: int, batch: int):
     from pdflow import scenes
     pairs = [scenes.make_pair(1000 + k, vga=True, n_objects=6) for k in range(n_distinct)]
@@ -186,6 +231,8 @@ def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    if "WORLD_SIZE" not in os.environ:
+        ws = args.gpus   # one process stands for the job: the CPU arm has no per-GPU work
     from oracle import oracle
     from pdflow import scenes
     i1, z1, i2, z2 = scenes.make_pair(1000, vga=True, n_objects=6)
@@ -756,9 +803,15 @@ def main():
     ap.add_argument("--iter-scale", type=float, default=0.75)
     ap.add_argument("--energy-margin", type=float, default=0.01)
     ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--replica-selftest", action="store_true",
+                    help="host-only check of the replica path (synthetic times over gloo)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ and args.impl == "ours":
+        return spawn_replicas(args.gpus, sys.argv[1:])
+    if args.replica_selftest:
+        return replica_selftest(args)
     if args.impl == "reference":
         return reference_arm(args)
     return ours(args)

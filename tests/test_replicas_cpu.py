@@ -44,6 +44,26 @@ def test_replicas_report_all_pairs_over_the_slowest_rank():
             assert value == pytest.approx(2 * 64 * 10 / 1.5)
 
 
+def test_bench_gpus_flag_spawns_the_replicas_itself():
+    """`python bench.py --gpus 2` outside torchrun starts two ranks with the
+    torchrun environment and prints one line for the two-rank job (checked
+    with synthetic per-rank times over gloo)."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--replica-selftest",
+                        "--batch", "8", "--steps", "5"], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2
+    assert line["ms_per_step"] == pytest.approx(200.0 / 5)        # the slower rank: 200 ms
+    assert line["value"] == pytest.approx(2 * 8 * 5 / 0.2)
+
+
 def test_single_process_is_its_own_job():
     import bench
     value, slowest = bench.replica_value(torch, 2000.0, pairs_per_rank=8, steps=5)
