@@ -292,6 +292,33 @@ int pdflow_solve_pair_noalloc(unsigned rows, unsigned width, unsigned height, co
                               const uint8_t* d_intensity1, const uint16_t* d_depth1, const uint8_t* d_intensity2,
                               const uint16_t* d_depth2, float* d_dx, float* d_dy, float* d_dz, void* stream);
 
+/* ---- Per-level record (copyAllSolutions after every level) ----
+ * The reference's live application copies every solved level's motion field
+ * and images to the host as the solve climbs the pyramid
+ * (scene_flow_visualization.cpp:194-199, CSF_cuda::copyAllSolutions,
+ * pdflow_cudalib.cu:224-237).  pdflow_keep_level_solutions(s, 1) makes every
+ * later solve record, per pair and per solved level, the median-filtered
+ * image-plane flow (du, dv in that level's pixels, dw in metres) and its
+ * motion field (computeMotionField at that level, pdflow_cudalib.cu:1150-1167,
+ * which uses the focal length of the finest solved width at every level).
+ * The record (6 planes per level per pair) is allocated by the first call
+ * that turns it on; 0 turns recording off.  Mixed-resolution handles refuse
+ * (PDFLOW_ERR_STATE).  Levels are numbered as the schedule visits them:
+ * 0 = the coarsest (15x20), ctf_levels - 1 = the finest (rows x cols); level
+ * i has (rows >> (L-1-i)) x (cols >> (L-1-i)) pixels, column-major. */
+int pdflow_keep_level_solutions(pdflow_solver* s, int keep);
+/* copyAllSolutions at solved level `level` for pair 0: its motion field and
+ * both frames' depth, intensity and back-projected xx, yy at that level's
+ * pyramid image (any pointer may be NULL; blocks).  Needs the record. */
+int pdflow_read_level_solutions(pdflow_solver* s, unsigned level, float* dx, float* dy, float* dz, float* depth,
+                                float* depth_old, float* colour, float* colour_old, float* xx, float* xx_old,
+                                float* yy, float* yy_old);
+/* Pair `pair`'s record at solved level `level`: image-plane flow (du, dv, dw;
+ * the reference's du_l, dv_l, dw_l after filterSolution) and motion field
+ * (dx, dy, dz); any pointer may be NULL; blocks. */
+int pdflow_read_level_flow(pdflow_solver* s, unsigned pair, unsigned level, float* du, float* dv, float* dw,
+                           float* dx, float* dy, float* dz);
+
 /* Human-readable text of the last error on this thread. */
 const char* pdflow_last_error(void);
 

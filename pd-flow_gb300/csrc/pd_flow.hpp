@@ -107,6 +107,22 @@ public:
               "pdflow_read_all_solutions");
     }
 
+    // The live application's per-level copy (scene_flow_visualization.cpp:194-199):
+    // keepLevelSolutions(true) before solveSceneFlowGPU records every level;
+    // copyAllSolutions(level, ...) then returns solved level `level` (0 = the
+    // coarsest) with that level's pyramid images.
+    void keepLevelSolutions(bool keep)
+    {
+        check(pdflow_keep_level_solutions(handle_, keep ? 1 : 0), "pdflow_keep_level_solutions");
+    }
+    void copyAllSolutions(unsigned level, float* dx, float* dy, float* dz, float* depth, float* depth_old,
+                          float* colour, float* colour_old, float* xx, float* xx_old, float* yy, float* yy_old)
+    {
+        check(pdflow_read_level_solutions(handle_, level, dx, dy, dz, depth, depth_old, colour, colour_old, xx,
+                                          xx_old, yy, yy_old),
+              "pdflow_read_level_solutions");
+    }
+
     void freeGPUMemory()
     {
         if (handle_) pdflow_destroy(handle_);

@@ -78,6 +78,72 @@ int pdflow_read_all_solutions(pdflow_solver* s, float* dx, float* dy, float* dz,
     return check_status(s);
 }
 
+int pdflow_keep_level_solutions(pdflow_solver* s, int keep)
+{
+    if (!s) return fail(PDFLOW_ERR_ARG, "null handle");
+    if (s->mixed) return fail(PDFLOW_ERR_STATE, "a mixed-resolution handle keeps no per-level record");
+    keep = keep ? 1 : 0;
+    if (keep == s->keep_levels) return PDFLOW_OK;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fail("synchronize", e);
+    if (keep && !s->lvl_keep) {
+        const size_t stride = level_keep_offset(s, s->ctf_levels);
+        void* p = nullptr;
+        e = cudaMalloc(&p, sizeof(float) * stride * s->batch);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error_code(PDFLOW_ERR_OOM, "per-level record allocation", e);
+        }
+        e = cudaMemsetAsync(p, 0, sizeof(float) * stride * s->batch, s->stream);
+        if (e != cudaSuccess) {
+            cudaFree(p);
+            return fail("per-level record clear", e);
+        }
+        s->lvl_keep = static_cast<float*>(p);
+        s->lvl_keep_stride = stride;
+    }
+    // captured solves hold the old launch sequence
+    for (auto& g : s->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+    s->keep_levels = keep;
+    return PDFLOW_OK;
+}
+
+int pdflow_read_level_flow(pdflow_solver* s, unsigned pair, unsigned level, float* du, float* dv, float* dw,
+                           float* dx, float* dy, float* dz)
+{
+    if (!s) return fail(PDFLOW_ERR_ARG, "null handle");
+    if (pair >= s->batch || level >= s->ctf_levels) return fail(PDFLOW_ERR_ARG, "pair or level out of range");
+    if (!s->keep_levels || !s->lvl_keep)
+        return fail(PDFLOW_ERR_STATE, "per-level record off (pdflow_keep_level_solutions)");
+    const LevelGeom g = level_geom(s, level, nullptr);
+    const float* base = s->lvl_keep + size_t(pair) * s->lvl_keep_stride + level_keep_offset(s, level);
+    float* dst[6] = {du, dv, dw, dx, dy, dz};
+    for (int a = 0; a < 6; ++a)
+        if (dst[a]) {
+            cudaError_t e = cudaMemcpyAsync(dst[a], base + size_t(a) * g.N, sizeof(float) * g.N,
+                                            cudaMemcpyDeviceToHost, s->stream);
+            if (e != cudaSuccess) return fail("level record copy", e);
+        }
+    return check_status(s);
+}
+
+int pdflow_read_level_solutions(pdflow_solver* s, unsigned level, float* dx, float* dy, float* dz, float* depth,
+                                float* depth_old, float* colour, float* colour_old, float* xx, float* xx_old,
+                                float* yy, float* yy_old)
+{
+    if (!s) return fail(PDFLOW_ERR_ARG, "null handle");
+    if (level >= s->ctf_levels) return fail(PDFLOW_ERR_ARG, "level beyond the solved levels");
+    unsigned li = 0;
+    level_geom(s, level, &li);   // the pyramid level holding this solved level's images
+    int rc = pdflow_read_level_images(s, li, 1, colour, depth, xx, yy);
+    if (!rc) rc = pdflow_read_level_images(s, li, 0, colour_old, depth_old, xx_old, yy_old);
+    if (rc) return rc;
+    if (!dx && !dy && !dz) return PDFLOW_OK;
+    return pdflow_read_level_flow(s, 0, level, nullptr, nullptr, nullptr, dx, dy, dz);
+}
+
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 {
     if (!s || !fn) return fail(PDFLOW_ERR_ARG, "null argument");

@@ -31,6 +31,9 @@ struct pdflow_solver {
     double* energy_part = nullptr;       // energy partial sums [batch][1024]
     float* sol_keep = nullptr;           // learned path: the plain 60x80 solutions [slot][10][4800] and ...
     unsigned* map2 = nullptr;            // ... a second slot map [batch] (one allocation, on first use)
+    int keep_levels = 0;                 // record every solved level's solution (pdflow_keep_level_solutions)
+    float* lvl_keep = nullptr;           // per slot: per level du, dv, dw, dx, dy, dz planes (on first use)
+    size_t lvl_keep_stride = 0;          // floats per slot of lvl_keep
     pdflow::LevelConsts L{};
     pdflow::State S{};
     float* alt[10] = {};                 // second buffer of du_acc,dv_acc,dw_acc,pd,puu,puv,pvu,pvv,pwu,pwv
@@ -101,6 +104,8 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
 int enqueue_energy(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, float* out,
                    const unsigned* map = nullptr);
 unsigned scaled_iters(unsigned iters, float scale);
+// Float offset of level `level`'s six planes in a slot of the per-level record.
+size_t level_keep_offset(const pdflow_solver* s, unsigned level);
 // Runs fn(s, stream, pairs, ctx) on the handle's stream, through a cached CUDA
 // graph keyed by (new frame slot, pairs, iteration form, kind) in graph mode.
 // Whatever fn reads from ctx is baked into the graph: equal kinds must mean

@@ -602,6 +602,31 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     }
 }
 
+// Per-level record of a solve (copyAllSolutions of the live application,
+// called after every level: scene_flow_visualization.cpp:194-199).
+__global__ void k_level_keep(LevelGeom g, LevelSol sol, PyrLevel o, Params p, float* __restrict__ keep,
+                             size_t stride, size_t off)
+{
+    const unsigned y = blockIdx.y;
+    const size_t po = pair_off(g.map, g.pstride, y);
+    const unsigned slot = g.map ? (__ldg(g.map + y) & kMapSlotMask) : y;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    sol = at(sol, po);
+    o = at(o, po);
+    float* k = keep + (size_t)slot * stride + off;
+    const float du = sol.du[i], dv = sol.dv[i], dw = sol.dw[i];
+    k[i] = du;
+    k[g.N + i] = dv;
+    k[2 * g.N + i] = dw;
+    const float z = o.dep[i];
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    if (z > 0.f) motion_field(z, du, dv, dw, o.xx[i], o.yy[i], inv_focal(p.fovh, p.cols), dx, dy, dz);
+    k[3 * g.N + i] = dx;
+    k[4 * g.N + i] = dy;
+    k[5 * g.N + i] = dz;
+}
+
 // Frame t's pyramid level becomes frame t-1's, for the mapped slots (float4
 // copies; level planes are 16-byte aligned and padded to whole float4s).
 __global__ void k_pyr_copy(PyrLevel src, PyrLevel dst, unsigned n, size_t pstride, const unsigned* __restrict__ map)
@@ -761,6 +786,13 @@ cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool la
 cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old, cudaStream_t st)
 {
     k_saturate<<<level_grid(g), kBlock, 0, st>>>(g, L, S, depth_old);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level_keep(LevelGeom g, LevelSol sol, PyrLevel old_l, Params p, float* keep, size_t stride,
+                              size_t off, cudaStream_t st)
+{
+    k_level_keep<<<level_grid(g), kBlock, 0, st>>>(g, sol, old_l, p, keep, stride, off);
     return cudaGetLastError();
 }
 

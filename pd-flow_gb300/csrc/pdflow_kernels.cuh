@@ -153,6 +153,12 @@ cudaError_t launch_dual(LevelGeom g, LevelConsts L, State S, Params p, cudaStrea
 cudaError_t launch_primal(LevelGeom g, LevelConsts L, State S, Params p, bool last, const float* depth_old,
                           cudaStream_t st);
 cudaError_t launch_saturate(LevelGeom g, LevelConsts L, State S, const float* depth_old, cudaStream_t st);
+// Copies level g's median output (du, dv, dw) and its motion field (the
+// reference's computeMotionField at that level: focal length of the finest
+// solved width p.cols, pdflow_cudalib.cu:1150-1167) into keep + slot * stride
+// + off: six planes of g.N floats (du, dv, dw, dx, dy, dz).
+cudaError_t launch_level_keep(LevelGeom g, LevelSol sol, PyrLevel old_l, Params p, float* keep, size_t stride,
+                              size_t off, cudaStream_t st);
 // `alt`: the second state buffers, read instead of S by pairs whose map entry
 // carries kMapAlt (mixed batches); kMapFinest marks a pair's finest level.
 cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts L, State S, LevelSol out,

@@ -158,6 +158,16 @@ int enqueue_pyramid(pdflow_solver* s, cudaStream_t st, unsigned pairs, const uns
     return PDFLOW_OK;
 }
 
+size_t level_keep_offset(const pdflow_solver* s, unsigned level)
+{
+    size_t off = 0;
+    for (unsigned k = 0; k < level; ++k) {
+        const LevelGeom g = level_geom(s, k, nullptr);
+        off += 6 * size_t(g.N);
+    }
+    return off;
+}
+
 unsigned scaled_iters(unsigned iters, float scale)
 {
     if (scale >= 1.f) return iters;
@@ -369,6 +379,11 @@ int enqueue_solve(pdflow_solver* s, cudaStream_t st, unsigned pairs, const Solve
                                nullptr, steps_hold_ddt_sq(steps)),
                  "median launch");
         ++count;
+        if (s->keep_levels && s->lvl_keep) {
+            CUDA_TRY(launch_level_keep(g, s->sol, o, p, s->lvl_keep, s->lvl_keep_stride, level_keep_offset(s, i), st),
+                     "level record launch");
+            ++count;
+        }
         if (int(i) == plan.energy_level && plan.energy) {
             s->launches = 0;
             rc = enqueue_energy(s, st, pairs, i, plan.energy, plan.map);
@@ -563,6 +578,7 @@ int pdflow_destroy(pdflow_solver* s)
     if (s->map_table) cudaFree(s->map_table);
     if (s->stage_rgb) cudaFree(s->stage_rgb);
     if (s->sol_keep) cudaFree(s->sol_keep);
+    if (s->lvl_keep) cudaFree(s->lvl_keep);
     cudaFree(s->arena);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
@@ -575,6 +591,7 @@ size_t pdflow_device_bytes(const pdflow_solver* s)
     size_t b = s->arena_bytes;   // plus the buffers allocated on first use
     if (s->sol_keep) b += learned_keep_bytes(s->batch);
     if (s->stage_rgb) b += size_t(s->width) * s->height * 3 * s->batch;
+    if (s->lvl_keep) b += sizeof(float) * s->lvl_keep_stride * s->batch;
     return b;
 }
 

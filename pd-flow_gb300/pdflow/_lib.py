@@ -178,6 +178,9 @@ _SIGNATURES = {
     "pdflow_set_level_form": (ctypes.c_int, [vp, u32, ctypes.c_int, u32]),
     "pdflow_autotune": (ctypes.c_int, [vp, u32, u32, ctypes.POINTER(TuneReport)]),
     "pdflow_read_all_solutions": (ctypes.c_int, [vp] + [vp] * 11),
+    "pdflow_keep_level_solutions": (ctypes.c_int, [vp, ctypes.c_int]),
+    "pdflow_read_level_solutions": (ctypes.c_int, [vp, u32] + [vp] * 11),
+    "pdflow_read_level_flow": (ctypes.c_int, [vp, u32, u32] + [vp] * 6),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "pdflow_set_quad_prefetch": (ctypes.c_int, [ctypes.c_uint]),
     "pdflow_debug_wait_timeout": (ctypes.c_int, [vp, u32]),
@@ -291,6 +294,26 @@ class _Extras:
         for c in range(3):
             for k in range(n):
                 device_to_host(ptrs[c].value + k * stride, out[c][k])
+        return out
+
+    def keep_level_solutions(self, keep: bool = True):
+        """Record every solved level's flow from the next solve on
+        (pdflow_keep_level_solutions; copyAllSolutions after every level)."""
+        check(load().pdflow_keep_level_solutions(self.handle, int(keep)), "pdflow_keep_level_solutions")
+
+    def level_shape(self, level: int):
+        """(rows, cols) of solved level `level` (0 = coarsest 15x20)."""
+        levels = (self.rows // 15).bit_length()
+        return self.rows >> (levels - 1 - level), self.cols >> (levels - 1 - level)
+
+    def level_flow(self, level: int, pair: int = 0):
+        """Pair `pair`'s record at solved level `level`: du, dv, dw (image
+        plane) and dx, dy, dz (motion field), each rows_l*cols_l floats."""
+        r, c = self.level_shape(level)
+        names = ("du", "dv", "dw", "dx", "dy", "dz")
+        out = {k: np.zeros(r * c, np.float32) for k in names}
+        check(load().pdflow_read_level_flow(self.handle, pair, level, *[_ptr(out[k]) for k in names]),
+              "pdflow_read_level_flow")
         return out
 
     def pair_stride(self) -> int:
@@ -412,6 +435,16 @@ class Solver(_Extras):
         names = ("dx", "dy", "dz", "depth", "depth_old", "colour", "colour_old", "xx", "xx_old", "yy", "yy_old")
         out = {k: np.zeros(n, np.float32) for k in names}
         check(load().pdflow_read_all_solutions(self._h, *[_ptr(out[k]) for k in names]), "pdflow_read_all_solutions")
+        return out
+
+    def level_solutions(self, level: int):
+        """copyAllSolutions at solved level `level` (pdflow_read_level_solutions;
+        needs keep_level_solutions before the solve)."""
+        r, c = self.level_shape(level)
+        names = ("dx", "dy", "dz", "depth", "depth_old", "colour", "colour_old", "xx", "xx_old", "yy", "yy_old")
+        out = {k: np.zeros(r * c, np.float32) for k in names}
+        check(load().pdflow_read_level_solutions(self._h, level, *[_ptr(out[k]) for k in names]),
+              "pdflow_read_level_solutions")
         return out
 
     def debug_solve(self):
