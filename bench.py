@@ -753,22 +753,34 @@ def mixed_batch_run(torch, steps=5, n=64, seed0=5_000_000):
     b = MixedBatch(n)
     b.push(rows, [f[0] for f in frames], [f[1] for f in frames])
     b.push(rows, [f[2] for f in frames], [f[3] for f in frames])
-    for _ in range(3):
-        b.solve()
-    b.synchronize()
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    t0.record()
-    for _ in range(steps):
-        b.solve()
-    b.synchronize()
-    t1.record()
-    torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1) / steps
+
+    def timed_ms():
+        for _ in range(3):
+            b.solve()
+        b.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record()
+        for _ in range(steps):
+            b.solve()
+        b.synchronize()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / steps
+
+    untuned_ms = timed_ms()
+    untuned = [b.flow(k) for k in range(n)]
+    tuned = b.autotune()
+    ms = timed_ms()
+    same = all(np.array_equal(x.view(np.uint32), y.view(np.uint32))
+               for k in range(n) for x, y in zip(b.flow(k), untuned[k]))
     b.close()
     counts = {r: rows.count(r) for r in (60, 120, 240, 480)}
     return {"pairs_s": n / (ms / 1000.0), "ms_per_batch": ms, "pairs": n, "rows_counts": counts,
-            "workload": "plain schedule, rows uniform in {60,120,240,480}, one launch per kernel per level size"}
+            "autotuned": [{k: v for k, v in t.items() if k != "ms_per_iter"} for t in tuned],
+            "untuned_pairs_s": n / (untuned_ms / 1000.0), "tuned_equals_untuned_bits": same,
+            "workload": "plain schedule, rows uniform in {60,120,240,480}, one launch per kernel per level size, "
+                        "tile form and iterations per launch autotuned per level size"}
 
 
 def reference_cuda_timing():

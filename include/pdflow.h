@@ -236,7 +236,11 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * with rows % 4 == 0).  pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The
- * handle's solution state is overwritten (the pushed frames are kept). */
+ * handle's solution state is overwritten (the pushed frames are kept).  On a
+ * mixed-resolution handle (pdflow_create_mixed) it tunes per coarse-to-fine
+ * step (report level i = the 15*2^i x 20*2^i step) over the pairs active at
+ * that step, among the tile forms 3..8 (2, 3 or 4 iterations per launch);
+ * pdflow_solve_mixed then runs each step in its chosen form. */
 #define PDFLOW_TUNE_CANDIDATES 23     /* form 0, form 1, forms 2..8 x {2, 3, 4} iterations per launch */
 typedef struct pdflow_tune_level {
     int form;                         /* chosen form */

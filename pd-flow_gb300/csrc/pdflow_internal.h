@@ -74,9 +74,11 @@ struct pdflow_solver {
     std::vector<unsigned> mixed_rows;    // rows of the pair in each slot (0: none)
     unsigned* map_table = nullptr;       // device: the slot maps of every launch of the mixed plan
     size_t map_table_cap = 0;
-    std::vector<unsigned> plan_rows;     // rows vector the current table / graph were built for
+    std::vector<unsigned> plan_rows;     // rows vector + per-step choices the current table / graph were built for
     cudaGraphExec_t mixed_graph = nullptr;
     int mixed_graph_slot = -1;
+    int mixed_form[8] = {-1, -1, -1, -1, -1, -1, -1, -1};   // per coarse-to-fine step: tile form (-1: the handle's)
+    unsigned mixed_kk[8] = {};           // per step: iterations per tile launch (0: 4)
 };
 
 namespace pdflow {
@@ -133,6 +135,9 @@ inline size_t learned_keep_bytes(unsigned batch)
 int learned_solve_all_fallback(pdflow_solver* s, unsigned n, const unsigned* slots, ::pdflow_net* net,
                                const ::pdflow_learned_opts* opts);
 int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, unsigned level, unsigned iters);
+// Autotuner of a mixed-resolution handle (pdflow_mixed.cu): per coarse-to-fine
+// step, the tile form and iterations per launch over the pairs active there.
+int mixed_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_tune_report* report);
 int check_status(pdflow_solver* s);
 void set_last_error(const char* text);   // the text pdflow_last_error returns on this thread
 LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, unsigned pairs = 1);

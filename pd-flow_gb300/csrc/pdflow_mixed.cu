@@ -10,11 +10,15 @@
 // launch ends the pair's level (its iteration count: 100 at its finest level,
 // 15 fewer per coarser one), which state buffer its level ended in, and
 // whether the step is its finest level (motion field).  The per-launch maps of
-// the whole solve are built on the host once per rows vector, uploaded as one
-// table, and the solve is replayed as one CUDA graph.
+// the whole solve are built on the host once per rows vector (and per-step
+// launch choice), uploaded as one table, and the solve is replayed as one CUDA
+// graph.  Each step's iterations run in the tile form and iterations per
+// launch that pdflow_autotune picked for it over the pairs active at that step
+// (mixed_autotune), by default the handle's paired tiles with 4 iterations.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "../../include/pdflow.h"
@@ -40,8 +44,45 @@ struct LaunchRec {
     unsigned step, kk, off, count;
 };
 
+// Iterations per tile launch at step i (the autotuned choice, else 4).
+unsigned step_kk(const pdflow_solver* s, unsigned i)
+{
+    const unsigned k = s->mixed_kk[i];
+    return (k >= 1 && k <= 4) ? k : 4u;
+}
+
+// Tile form at step i: the autotuned choice, else the handle's paired form
+// (forms 7 and 8 need rows % 4 == 0, levels 15x20 and 30x40 run form 5).
+int step_form(const pdflow_solver* s, unsigned i, const LevelGeom& g)
+{
+    int f = s->mixed_form[i] >= 3 ? s->mixed_form[i] : (s->iter_form >= 3 ? s->iter_form : 5);
+    if (f >= 7 && !quads_eligible(g, s->L, s->S, s->S)) f = 5;
+    return f;
+}
+
+LevelGeom step_geom(const pdflow_solver* s, unsigned step, unsigned pairs, const unsigned* map)
+{
+    const unsigned R = 15u << step, C = 20u << step;
+    LevelGeom g{R, C, R * C};
+    g.pairs = pairs;
+    g.pstride = s->pair_stride;
+    g.slots = s->batch;
+    g.map = map;
+    return g;
+}
+
+// kk iterations of the pairs of `g` in form `form`, state from cur to nxt.
+cudaError_t launch_step_tiles(pdflow_solver* s, const LevelGeom& g, const State& cur, const State& nxt,
+                              const Params& p, const PyrLevel& o, unsigned kk, cudaStream_t st, int form)
+{
+    if (form == 8) return launch_iterate_stream(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status, s->num_sms);
+    if (form == 7) return launch_iterate_quads(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status);
+    return launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, false, st, form - 3, s->status);
+}
+
 // The launches of a solve and their slot maps (flags in the high bits).
-void build_plan(const std::vector<unsigned>& rows, std::vector<LaunchRec>& plan, std::vector<unsigned>& table)
+void build_plan(const pdflow_solver* s, const std::vector<unsigned>& rows, std::vector<LaunchRec>& plan,
+                std::vector<unsigned>& table)
 {
     plan.clear();
     table.clear();
@@ -56,7 +97,7 @@ void build_plan(const std::vector<unsigned>& rows, std::vector<LaunchRec>& plan,
         std::vector<unsigned> remaining(act.size()), launches(act.size(), 0);
         for (size_t a = 0; a < act.size(); ++a) remaining[a] = 100u - 15u * (levels_of(rows[act[a]]) - 1u - i);
         for (;;) {
-            unsigned kk = 4, live = 0;
+            unsigned kk = step_kk(s, i), live = 0;
             for (unsigned r : remaining)
                 if (r > 0) {
                     kk = std::min(kk, r);
@@ -78,37 +119,69 @@ void build_plan(const std::vector<unsigned>& rows, std::vector<LaunchRec>& plan,
     }
 }
 
-int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec>& plan, unsigned* count)
+// Builds the plan of `rows` with the handle's per-step choices; uploads its
+// map table and drops the captured graph when the rows or the choices changed.
+int prepare_plan(pdflow_solver* s, const std::vector<unsigned>& rows, std::vector<LaunchRec>& plan)
+{
+    std::vector<unsigned> table;
+    build_plan(s, rows, plan, table);
+    std::vector<unsigned> sig(rows);
+    for (unsigned i = 0; i < kSteps; ++i) {
+        sig.push_back(step_kk(s, i));
+        sig.push_back(unsigned(s->mixed_form[i] + 1));
+    }
+    if (sig == s->plan_rows) return PDFLOW_OK;
+    if (table.size() > s->map_table_cap) {
+        if (s->map_table) cudaFree(s->map_table);
+        s->map_table = nullptr;
+        s->map_table_cap = 0;
+        cudaError_t e = cudaMalloc(&s->map_table, sizeof(unsigned) * table.size());
+        if (e != cudaSuccess) return set_error_code(PDFLOW_ERR_OOM, "map table", e);
+        s->map_table_cap = table.size();
+    }
+    cudaError_t e = cudaMemcpyAsync(s->map_table, table.data(), sizeof(unsigned) * table.size(),
+                                    cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "map table upload", e);
+    if (s->mixed_graph) cudaGraphExecDestroy(s->mixed_graph);
+    s->mixed_graph = nullptr;
+    s->plan_rows = sig;
+    return PDFLOW_OK;
+}
+
+// Launches plan[0, end) (the whole plan by default).  all_steps: the set-ups
+// write every step-size plane (the autotuner then runs any form on them).
+int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec>& plan, unsigned* count,
+                  size_t end = ~size_t(0), bool all_steps = false)
 {
     Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
     const int fn = s->new_slot, fo = fn ^ 1;
     const State alt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
                     s->alt[5], s->alt[6], s->alt[7], s->alt[8], s->alt[9]};
     State cur = s->S, nxt = alt;
-    for (const LaunchRec& r : plan) {
-        const unsigned R = 15u << r.step, C = 20u << r.step;
-        LevelGeom g{R, C, R * C};
-        g.pairs = r.count;
-        g.pstride = s->pair_stride;
-        g.slots = s->batch;
-        g.map = s->map_table + r.off;
+    for (size_t q = 0; q < plan.size() && q < end; ++q) {
+        const LaunchRec& r = plan[q];
+        const LevelGeom g = step_geom(s, r.step, r.count, s->map_table + r.off);
+        const int form = step_form(s, r.step, g);
         const unsigned li = kSteps - 1 - r.step;
         const PyrLevel o = s->pyr[fo][li], n = s->pyr[fn][li];
         cudaError_t e = cudaSuccess;
         if (r.kind == 0) {
             e = launch_level_init(g, r.step == 0, s->sol, o, n, s->L, s->S, st);
             if (e == cudaSuccess) e = launch_im_gradients(g, n, s->L, st);
-            if (e == cudaSuccess) e = launch_warp_steps(g, o, n, s->L, p, st, false);   // tiles only
+            if (e == cudaSuccess)
+                e = launch_warp_steps(g, o, n, s->L, p, st,
+                                      all_steps ? kStepsAll : (form >= 7 ? kStepsQuads : kStepsNone));
             *count += 3;
             cur = s->S;
             nxt = alt;
         } else if (r.kind == 1) {
-            const int shape = s->iter_form >= 3 ? s->iter_form - 3 : 2;   // the paired tiles of the handle's form
-            e = launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, r.kk, false, st, shape, s->status);
+            e = launch_step_tiles(s, g, cur, nxt, p, o, r.kk, st, form);
             std::swap(cur, nxt);
             *count += 1;
         } else {
-            e = launch_median(g, false, o, s->L, s->S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st, &alt, true);
+            e = launch_median(g, false, o, s->L, s->S, s->sol, s->dx, s->dy, s->dz, p, nullptr, st, &alt,
+                              !all_steps);
             *count += 1;
         }
         if (e != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "mixed batch launch", e);
@@ -117,6 +190,97 @@ int enqueue_mixed(pdflow_solver* s, cudaStream_t st, const std::vector<LaunchRec
 }
 
 }  // namespace
+
+// Per coarse-to-fine step i: replay the plan through step i's set-up (earlier
+// steps with the choices made so far), then time every tile form and
+// iterations per launch on the pairs active at step i (probe_iters
+// iterations, best of three runs after a warm-up) and keep the fastest.
+int pdflow::mixed_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_tune_report* report)
+{
+    if (n == 0 || n > s->batch) return set_error_code(PDFLOW_ERR_ARG, "pair count out of range");
+    if (s->frames < 2) return set_error_code(PDFLOW_ERR_STATE, "autotuning needs two frames pushed");
+    std::vector<unsigned> rows(s->mixed_rows.begin(), s->mixed_rows.begin() + n);
+    for (unsigned r : rows)
+        if (!r) return set_error_code(PDFLOW_ERR_STATE, "a pair of the batch has no frames");
+    if (probe_iters == 0) probe_iters = 12;
+    for (unsigned i = 0; i < 8; ++i) {
+        s->mixed_form[i] = -1;
+        s->mixed_kk[i] = 0;
+    }
+    std::vector<LaunchRec> plan;
+    int rc = prepare_plan(s, rows, plan);
+    if (rc) return rc;
+    Params p{s->prm.lambda_i, s->prm.lambda_d, s->prm.mu, s->prm.fovh, s->cols};
+    const State alt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
+                    s->alt[5], s->alt[6], s->alt[7], s->alt[8], s->alt[9]};
+    pdflow_tune_report rep{};
+    rep.levels = kSteps;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (unsigned i = 0; i < kSteps && rc == PDFLOW_OK; ++i) {
+        for (int c = 0; c < PDFLOW_TUNE_CANDIDATES; ++c) rep.level[i].ms_per_iter[c] = NAN;
+        rep.level[i].form = -1;
+        size_t q = 0;
+        while (q < plan.size() && !(plan[q].kind == 0 && plan[q].step == i)) ++q;
+        if (q == plan.size()) continue;   // no pair has this level
+        unsigned cnt = 0;
+        rc = enqueue_mixed(s, s->stream, plan, &cnt, q + 1, true);
+        if (rc) break;
+        const LevelGeom g = step_geom(s, i, plan[q].count, s->map_table + plan[q].off);
+        const PyrLevel o = s->pyr[s->new_slot ^ 1][kSteps - 1 - i];
+        float best = INFINITY;
+        int best_form = 5;
+        unsigned best_kk = 4;
+        int c = 0;
+        for (int form = 0; form <= 8; ++form)
+            for (unsigned kk : {0u, 2u, 3u, 4u}) {
+                if ((form <= 1) != (kk == 0)) continue;   // the candidate list of pdflow_tune.cu
+                const int idx = c++;
+                if (form < 3) continue;                   // mixed steps run tile forms only
+                if (form >= 7 && !quads_eligible(g, s->L, s->S, s->S)) continue;
+                float t = INFINITY;
+                for (int r = 0; r < 4 && rc == PDFLOW_OK; ++r) {
+                    cudaEventRecord(e0, s->stream);
+                    State cur = s->S, nxt = alt;
+                    for (unsigned done = 0; done < probe_iters;) {
+                        const unsigned k = std::min(kk, probe_iters - done);
+                        const cudaError_t e = launch_step_tiles(s, g, cur, nxt, p, o, k, s->stream, form);
+                        if (e != cudaSuccess) {
+                            rc = set_error_code(PDFLOW_ERR_CUDA, "mixed autotune launch", e);
+                            break;
+                        }
+                        std::swap(cur, nxt);
+                        done += k;
+                    }
+                    cudaEventRecord(e1, s->stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (r > 0 && ms < t) t = ms;
+                }
+                if (rc) break;
+                rep.level[i].ms_per_iter[idx] = t / float(probe_iters);
+                if (t < best) {
+                    best = t;
+                    best_form = form;
+                    best_kk = kk;
+                }
+            }
+        s->mixed_form[i] = best_form;
+        s->mixed_kk[i] = best_kk;
+        rep.level[i].form = best_form;
+        rep.level[i].iters_per_launch = best_kk;
+        rc = rc ? rc : prepare_plan(s, rows, plan);   // later steps replay with this step's choice
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    rc = check_status(s);
+    if (rc) return rc;
+    if (report) *report = rep;
+    return PDFLOW_OK;
+}
 
 extern "C" {
 
@@ -221,25 +385,8 @@ int pdflow_solve_mixed(pdflow_solver* s, unsigned n)
             return PDFLOW_ERR_STATE;
         }
     std::vector<LaunchRec> plan;
-    std::vector<unsigned> table;
-    build_plan(rows, plan, table);
-    const bool replan = rows != s->plan_rows;
-    if (replan) {
-        if (table.size() > s->map_table_cap) {
-            if (s->map_table) cudaFree(s->map_table);
-            s->map_table = nullptr;
-            cudaError_t e = cudaMalloc(&s->map_table, sizeof(unsigned) * table.size());
-            if (e != cudaSuccess) return set_error_code(PDFLOW_ERR_OOM, "map table", e);
-            s->map_table_cap = table.size();
-        }
-        cudaError_t e = cudaMemcpyAsync(s->map_table, table.data(), sizeof(unsigned) * table.size(),
-                                        cudaMemcpyHostToDevice, s->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        if (e != cudaSuccess) return set_error_code(PDFLOW_ERR_CUDA, "map table upload", e);
-        if (s->mixed_graph) cudaGraphExecDestroy(s->mixed_graph);
-        s->mixed_graph = nullptr;
-        s->plan_rows = rows;
-    }
+    const int rc0 = prepare_plan(s, rows, plan);
+    if (rc0) return rc0;
     unsigned count = 0;
     if (!s->use_graph) {
         int rc = enqueue_mixed(s, s->stream, plan, &count);

@@ -52,7 +52,8 @@ int pdflow_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_t
         set_last_error("bad argument");
         return PDFLOW_ERR_ARG;
     }
-    if (s->frames < 2 || s->slot_mode || s->mixed) {
+    if (s->mixed) return mixed_autotune(s, n, probe_iters, report);
+    if (s->frames < 2 || s->slot_mode) {
         set_last_error("autotuning needs two frames pushed for the whole batch");
         return PDFLOW_ERR_STATE;
     }

@@ -650,6 +650,22 @@ class MixedBatch:
     def solve(self, n: int | None = None):
         check(load().pdflow_solve_mixed(self._h, n or len(self.rows)), "pdflow_solve_mixed")
 
+    def autotune(self, n: int | None = None, probe_iters: int = 12):
+        """Per coarse-to-fine step (15x20 .. 480x640), the tile form and
+        iterations per launch over the pairs active at that step
+        (pdflow_autotune on a mixed handle); returns [{step, form,
+        iters_per_launch, ms_per_iter}] for the steps some pair has."""
+        rep = TuneReport()
+        check(load().pdflow_autotune(self._h, n or len(self.rows), probe_iters, ctypes.byref(rep)), "pdflow_autotune")
+        out = []
+        for i in range(rep.levels):
+            if rep.level[i].form < 0:
+                continue
+            ms = [None if np.isnan(x) else float(x) for x in rep.level[i].ms_per_iter]
+            out.append({"step": f"{15 << i}x{20 << i}", "form": rep.level[i].form,
+                        "iters_per_launch": rep.level[i].iters_per_launch, "ms_per_iter": ms})
+        return out
+
     def flow(self, k: int):
         r = self.rows[k]
         out = [np.zeros(r * (r * 4 // 3), np.float32) for _ in range(3)]

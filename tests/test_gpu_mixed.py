@@ -36,6 +36,32 @@ def test_mixed_batch_pairs_equal_single_solves(built_lib, use_graph):
     b.close()
 
 
+def test_autotuned_mixed_batch_pairs_equal_single_solves(built_lib):
+    """The autotuner picks a tile form and iterations per launch per
+    coarse-to-fine step over the pairs active there; the tuned plan still gives
+    every pair its single-pair solve, bit for bit."""
+    rows = [480, 60, 240, 120, 480, 240, 30]
+    pairs = [scenes.make_pair(700 + k, vga=(r == 480), n_objects=1 + k % 5) for k, r in enumerate(rows)]
+    b = MixedBatch(8)
+    b.push(rows, [p[0] for p in pairs], [p[1] for p in pairs])
+    b.push(rows, [p[2] for p in pairs], [p[3] for p in pairs])
+    rep = b.autotune()
+    assert [r["step"] for r in rep] == ["15x20", "30x40", "60x80", "120x160", "240x320", "480x640"]
+    for r in rep:
+        assert r["form"] in (3, 4, 5, 6, 7, 8) and r["iters_per_launch"] in (2, 3, 4)
+        assert r["ms_per_iter"][0] is None                      # two kernels per iteration: not a mixed form
+        if r["step"] in ("15x20", "30x40"):
+            assert r["form"] <= 6                                # rows % 4 != 0: no register tiles
+    for _ in range(2):                                           # graph capture, then replay
+        b.solve()
+        for k, r in enumerate(rows):
+            got = b.flow(k)
+            ref = single(r, pairs[k])
+            for x, y in zip(got, ref):
+                assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (k, r)
+    b.close()
+
+
 def test_mixed_batch_rejects_bad_rows(built_lib):
     from pdflow import ERR_ARG, PDFlowError
     b = MixedBatch(2)
