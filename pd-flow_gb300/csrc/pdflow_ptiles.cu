@@ -7,9 +7,10 @@
 // step products) live in registers while its kk <= 4 iterations run: each of
 // the 512 threads owns a vertical pixel pair (rows 2p, 2p+1 of region column
 // c) and computes it with packed FP32x2 instructions.  Meanwhile the TMA unit
-// copies the next tile's 32 planes into a shared-memory staging buffer (one
-// tensor copy per plane, completing on an mbarrier), so the region loads run
-// behind the arithmetic instead of between launches' compute phases.
+// copies the next tile's 32 planes into a shared-memory staging buffer (two 4D
+// tensor copies, one per run of planes the arena keeps back to back: the 13
+// state planes and the 19 constants, pdflow_tmap.h; completing on an
+// mbarrier), so the region loads run behind the arithmetic.
 //
 // Neighbours: the row below the pair (dual step) and above it (primal step)
 // by warp shuffles inside the column's 16 lanes; the column to the right
@@ -27,6 +28,7 @@
 #include "pdflow_iterate.cuh"
 #include "pdflow_math.cuh"
 #include "pdflow_pack.cuh"
+#include "pdflow_tmap.h"
 
 namespace pdflow {
 
@@ -40,11 +42,11 @@ constexpr int kSR = kST + 2 * kSH;             // region rows and columns (32)
 constexpr int kSPlane = kSR * kSR;             // floats per shared plane
 constexpr int kSThreads = kSR * kSR / 2;       // one thread per pixel pair (512)
 
-// staging planes (TMA destinations, in this order): 13 state, 19 constants;
-// then the six exchange planes
+// staging planes (TMA destinations, in the arena's order): 13 state, 19
+// constants; then the six exchange planes
 enum { S_DU, S_DV, S_DW, S_UA, S_VA, S_WA, S_PD, S_PUU, S_PUV, S_PVU, S_PVV, S_PWU, S_PWV,
-       K_DUP, K_DVP, K_RI, K_RJ, K_DDT, K_DDU, K_DDV, K_S0, K_S1, K_S2, K_S3, K_S4,
-       K_MU, K_DCT, K_DCU, K_DCV, K_TU, K_TV, K_TW,
+       K_RI, K_RJ, K_DCT, K_DCU, K_DCV, K_DDT, K_DDU, K_DDV, K_MU, K_DUP, K_DVP,
+       K_S0, K_S1, K_S2, K_S3, K_S4, K_TU, K_TV, K_TW,
        N_STAGE,
        X_U = N_STAGE, X_V, X_W, Y_U, Y_V, Y_W, N_PLANES };
 
@@ -61,10 +63,10 @@ struct StreamArgs {
     unsigned* status;          // device word: kStreamTimeout when a bounded wait gives up
 };
 
-// 3D maps (rows, columns, arena slots) of the 13 source state planes and the
-// 19 constant planes, box = one region.
+// 4D maps (rows, columns, planes, arena slots) of the 13 source state planes
+// and of the 19 constant planes, box = one region of every plane of the group.
 struct StreamMaps {
-    CUtensorMap m[N_STAGE];
+    CUtensorMap state, consts;
 };
 
 constexpr unsigned kStreamTimeout = 0x5354524Du;
@@ -129,13 +131,16 @@ __device__ __forceinline__ void issue_region(const StreamArgs& a, const StreamMa
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
                  "r"((uint32_t)N_STAGE * (uint32_t)kSPlane * 4u)
                  : "memory");
-#pragma unroll
-    for (int k = 0; k < N_STAGE; ++k)
-        asm volatile(
-            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-            " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(sm + k * kSPlane)),
-            "l"(reinterpret_cast<uint64_t>(&tm.m[k])), "r"(t.rv0), "r"(t.ru0), "r"(slot), "r"(bar)
-            : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(sm + S_DU * kSPlane)),
+        "l"(reinterpret_cast<uint64_t>(&tm.state)), "r"(t.rv0), "r"(t.ru0), "r"(0), "r"(slot), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(sm + K_RI * kSPlane)),
+        "l"(reinterpret_cast<uint64_t>(&tm.consts)), "r"(t.rv0), "r"(t.ru0), "r"(0), "r"(slot), "r"(bar)
+        : "memory");
 }
 
 __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, const __grid_constant__ StreamMaps tm)
@@ -306,24 +311,6 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
     }
 }
 
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn stream_encoder()
-{
-    static const EncodeTiledFn fn = [] {
-        void* q = nullptr;
-        cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &q, 12000, cudaEnableDefault, &qr) !=
-                cudaSuccess ||
-            qr != cudaDriverEntryPointSuccess)
-            q = nullptr;
-        return reinterpret_cast<EncodeTiledFn>(q);
-    }();
-    return fn;
-}
-
 }  // namespace
 
 size_t stream_smem_bytes() { return sizeof(float) * N_PLANES * kSPlane; }
@@ -341,7 +328,7 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
                                   unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas)
 {
     // same preconditions as the quad tiles (16-byte aligned planes, rows % 4 == 0)
-    if (kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0 || !stream_encoder())
+    if (kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0)
         return cudaErrorInvalidValue;
     StreamArgs a;
     a.g = g;
@@ -356,21 +343,17 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     a.tiles_v = (g.R + kST - 1) / kST;
     a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
     a.total = a.tiles * g.pairs;
+    // the runs of planes (quads_eligible checked that each is equally spaced)
+    const float* sg[13] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,
+                           src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv};
+    const float* cg[19] = {L.ri, L.rj, L.dct, L.dcu, L.dcv, L.ddt, L.ddu, L.ddv, L.mu, L.du_prev, L.dv_prev,
+                           L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4], L.qs[5], L.qs[6], L.qs[7]};
+    size_t ss = 0, cs = 0;
     StreamMaps maps{};
-    const float* planes[N_STAGE] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,
-                                    src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv,
-                                    L.du_prev, L.dv_prev, L.ri, L.rj, L.ddt, L.ddu, L.ddv,
-                                    L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4],
-                                    L.mu, L.dct, L.dcu, L.dcv, L.qs[5], L.qs[6], L.qs[7]};
-    const cuuint64_t dims[3] = {g.R, g.C, g.slots};
-    const cuuint64_t strides[2] = {cuuint64_t(g.R) * 4u, g.pstride};
-    const cuuint32_t box[3] = {kSR, kSR, 1}, estr[3] = {1, 1, 1};
-    const EncodeTiledFn encode = stream_encoder();
-    for (int k = 0; k < N_STAGE; ++k)
-        if (encode(&maps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(planes[k]), dims, strides, box,
-                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return cudaErrorInvalidValue;
+    if (!equally_spaced(sg, 13, &ss) || !equally_spaced(cg, 19, &cs) ||
+        !encode_plane_group(&maps.state, sg[0], 13, ss, g.R, g.C, g.slots, g.pstride, kSR, kSR) ||
+        !encode_plane_group(&maps.consts, cg[0], 19, cs, g.R, g.C, g.slots, g.pstride, kSR, kSR))
+        return cudaErrorInvalidValue;
     const unsigned grid = ctas < a.total ? ctas : a.total;
     k_iterate_stream<<<grid, kSThreads, stream_smem_bytes(), st>>>(a, maps);
     return cudaGetLastError();

@@ -22,8 +22,9 @@
 // evaluates at that pixel (computeGradient and computeDivergence,
 // pdflow_cudalib.cu:935-1013), so the results are bit-identical to the other
 // iteration forms.  The 19 level constants (11 set-up planes plus the 8 step
-// products the warping kernel stores for this form) arrive in shared memory by
-// one TMA tensor copy per plane.
+// products the warping kernel stores for this form), which the arena keeps
+// back to back, arrive in shared memory by one 4D TMA tensor copy
+// (pdflow_tmap.h).
 //
 // Every pixel of the region is updated in every iteration; after j
 // iterations the ring of width j at a non-border region edge holds values
@@ -36,6 +37,7 @@
 
 #include "pdflow_iterate.cuh"
 #include "pdflow_math.cuh"
+#include "pdflow_tmap.h"
 
 namespace pdflow {
 
@@ -47,13 +49,12 @@ constexpr int kQR = kQT + 2 * kQH;             // region rows and columns (32)
 constexpr int kQPlane = kQR * kQR;             // floats per shared plane
 constexpr int kQThreads = kQR * kQR / 4;       // one thread per quad (256)
 
-// shared planes: the 19 constants (TMA destinations, in this order), then the
-// six exchange planes
-enum { C_DUP, C_DVP, C_RI, C_RJ, C_DDT, C_DDU, C_DDV, C_S0, C_S1, C_S2, C_S3, C_S4,    // dual step
-       C_MU, C_DCT, C_DCU, C_DCV, C_TU, C_TV, C_TW,                                    // primal step
+// shared planes: the 19 constants (one tensor copy; the arena's order), then
+// the six exchange planes
+enum { C_RI, C_RJ, C_DCT, C_DCU, C_DCV, C_DDT, C_DDU, C_DDV, C_MU, C_DUP, C_DVP,
+       C_S0, C_S1, C_S2, C_S3, C_S4, C_TU, C_TV, C_TW,
        C_NCONST,
        X_U = C_NCONST, X_V, X_W, Y_U, Y_V, Y_W, Q_NPLANES };
-constexpr int kDualPlanes = C_MU;              // the first group of tensor copies
 
 struct QuadArgs {
     LevelGeom g;
@@ -69,10 +70,10 @@ struct QuadArgs {
     unsigned* status;          // device word: kQuadTimeout when the bounded wait for the region gives up
 };
 
-// Tensor maps: the 19 constant planes (region loads), then the 13 source state
-// planes (L2 prefetches only; the state itself is loaded with 16-byte loads).
+// 4D tensor maps: the 19 constant planes (region loads) and the 13 source
+// state planes (L2 prefetches only; the state is loaded with 16-byte loads).
 struct QuadMaps {
-    CUtensorMap m[C_NCONST + 13];
+    CUtensorMap consts, state;
 };
 
 constexpr unsigned kQuadTimeout = 0x51554144u;
@@ -188,7 +189,7 @@ __device__ __forceinline__ void shrink(float& du, float& dv, float of, float th,
 __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, const __grid_constant__ QuadMaps tm)
 {
     extern __shared__ __align__(128) float sm[];   // TMA tensor copies land on 128-byte boundaries
-    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ __align__(8) unsigned long long bar[1];
     const unsigned y = blockIdx.y;
     const size_t po = pair_off(a.g.map, a.g.pstride, y);
     const int R = (int)a.g.R, C = (int)a.g.C;
@@ -201,46 +202,43 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
     const int u = ru0 + c, v0 = rv0 + 4 * q;        // the quad's image column and first row
     const bool live = u < C && v0 < R;              // v0 < R implies v0 + 3 < R (R % 4 == 0)
 
-    // ---- region load: constants by TMA (two groups), state by 16-byte loads ----
-    const uint32_t b0 = sm_addr(&bar[0]), b1 = sm_addr(&bar[1]);
+    // ---- region load: constants by one TMA tensor copy, state by 16-byte loads ----
+    const uint32_t b0 = sm_addr(&bar[0]);
     constexpr uint32_t kBox = (uint32_t)kQPlane * 4u;
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b0));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b0),
-                     "r"((uint32_t)kDualPlanes * kBox)
+                     "r"((uint32_t)C_NCONST * kBox)
                      : "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b1),
-                     "r"((uint32_t)(C_NCONST - kDualPlanes) * kBox)
-                     : "memory");
-        // box (32 rows, 32 columns, 1 slot) at (rv0, ru0, slot): rv0 is a multiple
-        // of 4 floats (16 bytes); rows and columns past the level arrive as zeros
+        // box (32 rows, 32 columns, 19 planes, 1 slot) at (rv0, ru0, 0, slot): rv0
+        // is a multiple of 4 floats (16 bytes); rows and columns past the level
+        // arrive as zeros
         const int slot = (int)(a.g.map ? (__ldg(a.g.map + y) & kMapSlotMask) : y);
-#pragma unroll
-        for (int k = 0; k < C_NCONST; ++k)
-            asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(sm_addr(sm + k * kQPlane)),
-                "l"(reinterpret_cast<uint64_t>(&tm.m[k])), "r"(rv0), "r"(ru0), "r"(slot), "r"(k < kDualPlanes ? b0 : b1)
-                : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(sm_addr(sm)),
+            "l"(reinterpret_cast<uint64_t>(&tm.consts)), "r"(rv0), "r"(ru0), "r"(0), "r"(slot), "r"(b0)
+            : "memory");
     }
     if (t == 32 && a.ahead) {
         // Warm L2 with the region of the CTA that takes over this launch slot:
         // CTAs start in launch order, so the one `ahead` positions later starts
-        // about when this one finishes.  One tensor prefetch per plane.
+        // about when this one finishes.  One tensor prefetch per plane group.
         const unsigned n = blockIdx.x + a.tiles * y + a.ahead;
         if (n < a.tiles * gridDim.y) {
             const unsigned ny = n / a.tiles, nx = n % a.tiles;
             const int ntv = (int)(nx % a.tiles_v), ntu = (int)(nx / a.tiles_v);
             const int nrv0 = max(ntv * kQT - kQH, 0), nru0 = max(ntu * kQT - kQH, 0);
             const int nslot = (int)(a.g.map ? (__ldg(a.g.map + ny) & kMapSlotMask) : ny);
-#pragma unroll
-            for (int k = 0; k < C_NCONST + 13; ++k)
-                asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
-                                 reinterpret_cast<uint64_t>(&tm.m[k])),
-                             "r"(nrv0), "r"(nru0), "r"(nslot)
-                             : "memory");
+            asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(
+                             reinterpret_cast<uint64_t>(&tm.consts)),
+                         "r"(nrv0), "r"(nru0), "r"(0), "r"(nslot)
+                         : "memory");
+            asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(
+                             reinterpret_cast<uint64_t>(&tm.state)),
+                         "r"(nrv0), "r"(nru0), "r"(0), "r"(nslot)
+                         : "memory");
         }
     }
     Q du{}, dv{}, dw{}, ua{}, va{}, wa{}, pd{}, puu{}, puv{}, pvu{}, pvv{}, pwu{}, pwv{};
@@ -287,7 +285,6 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
     const unsigned lane = t & 31u;
 
     wait_group(b0);
-    bool have_primal = false;
     for (unsigned j = 0; j < a.kk; ++j) {
         // ---------------- dual step (computeGradient + updateDualVariables) ----------------
         {
@@ -342,10 +339,6 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
             disc(pwu.lo.y, pwv.lo.y);
             disc(pwu.hi.x, pwv.hi.x);
             disc(pwu.hi.y, pwv.hi.y);
-        }
-        if (!have_primal) {
-            wait_group(b1);   // the primal step's constants
-            have_primal = true;
         }
         // ---------------- primal step (computeDivergence + updatePrimalVariables) ----------------
         {
@@ -418,7 +411,6 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
         // (X planes: written before the dual's barrier, read after it; Y planes the same
         // around the primal's barrier)
     }
-    if (!have_primal) wait_group(b1);   // kk == 0: leave no copy in flight
 
     // ---- write the interior ----
     if (live && v0 >= iv0 && v0 < iv1 && u >= iu0 && u < iu1) {
@@ -426,26 +418,6 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
 #pragma unroll
         for (int k = 0; k < 13; ++k) stg_q(at(a.dst[k], po) + gi, *st[k]);
     }
-}
-
-// cuTensorMapEncodeTiled through the runtime's driver entry-point query (the
-// library links no driver library); null: not available.
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn quad_encoder()
-{
-    static const EncodeTiledFn fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &qr) !=
-                cudaSuccess ||
-            qr != cudaDriverEntryPointSuccess)
-            p = nullptr;
-        return reinterpret_cast<EncodeTiledFn>(p);
-    }();
-    return fn;
 }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
@@ -466,18 +438,33 @@ cudaError_t prepare_quads()
     return e;
 }
 
+// The constant planes of the register-resident tiles, in their arena (and
+// shared-memory) order, and the state planes in State order.
+static void const_group(const LevelConsts& L, const float* out[19])
+{
+    const float* c[19] = {L.ri, L.rj, L.dct, L.dcu, L.dcv, L.ddt, L.ddu, L.ddv, L.mu, L.du_prev, L.dv_prev,
+                          L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4], L.qs[5], L.qs[6], L.qs[7]};
+    for (int k = 0; k < 19; ++k) out[k] = c[k];
+}
+static void state_group(const State& S, const float* out[13])
+{
+    const float* c[13] = {S.du, S.dv, S.dw, S.dua, S.dva, S.dwa, S.pd, S.puu, S.puv, S.pvu, S.pvv, S.pwu, S.pwv};
+    for (int k = 0; k < 13; ++k) out[k] = c[k];
+}
+
 bool quads_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst)
 {
-    if (g.R % 4u != 0 || g.pstride % 16u != 0 || g.slots == 0 || !quad_encoder()) return false;
-    const void* planes[] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd, src.puu, src.puv,
-                            src.pvu, src.pvv, src.pwu, src.pwv, dst.du, dst.dv, dst.dw, dst.dua, dst.dva,
-                            dst.dwa, dst.pd, dst.puu, dst.puv, dst.pvu, dst.pvv, dst.pwu, dst.pwv,
-                            L.du_prev, L.dv_prev, L.ri, L.rj, L.ddt, L.ddu, L.ddv, L.mu, L.dct, L.dcu, L.dcv};
-    for (const void* p : planes)
-        if (!aligned16(p)) return false;
-    for (const float* p : L.qs)
-        if (!aligned16(p)) return false;
-    return true;
+    if (g.R % 4u != 0 || g.pstride % 16u != 0 || g.slots == 0 || !tensor_map_encoder()) return false;
+    // the constants and both state buffers are runs of planes at one stride
+    const float* cg[19];
+    const float* sg[13];
+    const float* dg[13];
+    const_group(L, cg);
+    state_group(src, sg);
+    state_group(dst, dg);
+    size_t a = 0, b = 0, c = 0;
+    if (!equally_spaced(cg, 19, &a) || !equally_spaced(sg, 13, &b) || !equally_spaced(dg, 13, &c)) return false;
+    return aligned16(cg[0]) && aligned16(sg[0]) && aligned16(dg[0]);
 }
 
 cudaError_t launch_iterate_quads(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
@@ -503,23 +490,19 @@ cudaError_t launch_iterate_quads(LevelGeom g, LevelConsts L, State src, State ds
     a.tiles_v = (g.R + kQT - 1) / kQT;
     a.tiles = a.tiles_v * ((g.C + kQT - 1) / kQT);
     a.ahead = g_quad_ahead.load();
-    // 3D maps (rows, columns, arena slots) of the 19 constant planes and the 13
-    // source state planes, box = the whole region
+    // 4D maps (rows, columns, planes, arena slots): the 19 constant planes and the
+    // 13 source state planes, box = the whole region of every plane of the group
     QuadMaps maps{};
-    const float* cp[C_NCONST + 13] = {L.du_prev, L.dv_prev, L.ri, L.rj, L.ddt, L.ddu, L.ddv,
-                                      L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4],
-                                      L.mu, L.dct, L.dcu, L.dcv, L.qs[5], L.qs[6], L.qs[7],
-                                      src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,
-                                      src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv};
-    const cuuint64_t dims[3] = {g.R, g.C, g.slots};
-    const cuuint64_t strides[2] = {cuuint64_t(g.R) * 4u, g.pstride};
-    const cuuint32_t box[3] = {kQR, kQR, 1}, estr[3] = {1, 1, 1};
-    const EncodeTiledFn encode = quad_encoder();
-    for (int k = 0; k < C_NCONST + 13; ++k)
-        if (encode(&maps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(cp[k]), dims, strides, box,
-                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return cudaErrorInvalidValue;
+    const float* cg[19];
+    const float* sg[13];
+    const_group(L, cg);
+    state_group(src, sg);
+    size_t cs = 0, ss = 0;
+    equally_spaced(cg, 19, &cs);
+    equally_spaced(sg, 13, &ss);
+    if (!encode_plane_group(&maps.consts, cg[0], 19, cs, g.R, g.C, g.slots, g.pstride, kQR, kQR) ||
+        !encode_plane_group(&maps.state, sg[0], 13, ss, g.R, g.C, g.slots, g.pstride, kQR, kQR))
+        return cudaErrorInvalidValue;
     dim3 grid(a.tiles, g.pairs);
     k_iterate_quads<<<grid, kQThreads, quads_smem_bytes(), st>>>(a, maps);
     return cudaGetLastError();

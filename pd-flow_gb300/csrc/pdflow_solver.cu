@@ -113,11 +113,15 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     s->stage_Z = cv.plane(Nimg);
     const size_t N = size_t(s->rows) * s->cols;
     LevelConsts& L = s->L;
-    float** lp[] = {&L.ri, &L.rj, &L.ri2, &L.rj2, &L.dcu_aux, &L.dcv_aux, &L.ddu_aux, &L.ddv_aux, &L.dct,
-                    &L.dcu, &L.dcv, &L.ddt, &L.ddu, &L.ddv, &L.mu, &L.du_prev, &L.dv_prev, &L.spd, &L.spuvx,
-                    &L.spuvy, &L.spwx, &L.spwy, &L.tu, &L.tv, &L.tw};
+    // The 19 planes the register-resident tiles read come first and back to
+    // back (ri .. dv_prev, then the 8 step products), so that one 4D tensor
+    // copy moves a region of all of them (pdflow_tmap.h).
+    float** lp[] = {&L.ri,  &L.rj,      &L.dct,     &L.dcu,    &L.dcv,     &L.ddt,     &L.ddu,
+                    &L.ddv, &L.mu,      &L.du_prev, &L.dv_prev, &L.qs[0],  &L.qs[1],   &L.qs[2],
+                    &L.qs[3], &L.qs[4], &L.qs[5],   &L.qs[6],  &L.qs[7],  &L.ri2,     &L.rj2,
+                    &L.dcu_aux, &L.dcv_aux, &L.ddu_aux, &L.ddv_aux, &L.spd, &L.spuvx, &L.spuvy,
+                    &L.spwx, &L.spwy, &L.tu, &L.tv, &L.tw};
     for (float** p : lp) *p = cv.plane(N);
-    for (float*& p : L.qs) p = cv.plane(N);
     State& S = s->S;
     float** sp[] = {&S.du, &S.dv, &S.dw, &S.dua, &S.dva, &S.dwa, &S.pd, &S.puu, &S.puv, &S.pvu, &S.pvv, &S.pwu,
                     &S.pwv};
@@ -125,8 +129,9 @@ void carve_solver(pdflow_solver* s, char* base, size_t* used)
     LevelSol& O = s->sol;
     float** op[] = {&O.du, &O.dv, &O.dw, &O.pd, &O.puu, &O.puv, &O.pvu, &O.pvv, &O.pwu, &O.pwv};
     for (float** p : op) *p = cv.plane(N);
-    for (float*& p : s->alt) p = cv.plane(N);
+    // the second state buffer in the order of S (du dv dw, then the rest)
     for (float*& p : s->alt_d) p = cv.plane(N);
+    for (float*& p : s->alt) p = cv.plane(N);
     s->dx = cv.plane(N);
     s->dy = cv.plane(N);
     s->dz = cv.plane(N);
