@@ -274,19 +274,24 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(form):
-    """DRAM bytes per pixel-iteration of the 480x640 tile launch of iteration
-    form `form`, from the committed ncu summary (`bytes_per_px_iter_formN:`
-    lines), else None."""
-    key = f"bytes_per_px_iter_form{form}:"
-    try:
-        with open(os.path.join(ROOT, "profiles", "k_iterate_tiles2_forms_vga_batch16_480x640.md")) as f:
-            for line in f:
-                if line.startswith(key):
-                    return {"bytes_per_px_iter": float(line.split(":")[1]), "form": form}
-    except OSError:
-        pass
-    return None
+# Floats of one pixel's planes that a tile launch moves between DRAM and the
+# SMs, per iteration form: every launch reads each plane of the level once
+# (the halo's re-reads are L2 hits) and writes the 13 state planes once.
+#   forms 3-6 (shared-memory tiles): 13 state + 11 constants in, 13 out;
+#   forms 7, 8 (register tiles): 13 state + 19 constants (the 8 step products
+#   are loaded, not recomputed) in, 13 out.
+TILE_FLOATS_IN = {3: 24, 4: 24, 5: 24, 6: 24, 7: 32, 8: 32}
+TILE_FLOATS_OUT = 13
+KERNEL_OF_FORM = {3: "k_iterate_tiles2<40,40>", 4: "k_iterate_tiles2<40,34>", 5: "k_iterate_tiles2<24,24>",
+                  6: "k_iterate_tiles2<24,28>", 7: "k_iterate_quads", 8: "k_iterate_stream"}
+
+
+def tile_traffic_per_iteration(form: int, kk: int, pixels: int):
+    """DRAM bytes per iteration of a tile form at kk iterations per launch over
+    `pixels` pixels, from the launch geometry (None for non-tile forms)."""
+    if form not in TILE_FLOATS_IN or kk <= 0:
+        return None
+    return 4.0 * (TILE_FLOATS_IN[form] + TILE_FLOATS_OUT) * pixels / kk
 
 
 def replica_value(torch, total_ms: float, pairs_per_rank: int, steps: int, device=None):
@@ -317,12 +322,11 @@ def epe(a, b, valid):
     return np.array([d[k][valid[k]].mean() for k in range(d.shape[0])])
 
 
-def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
-    """16 camera streams (8 QVGA, 8 VGA) at `rate` Hz with Poisson arrivals
-    through the request loop, learned warm start on."""
-    from pdflow import datagen, scenes
-    from pdflow.serving import Server, simulate
-    T = int(seconds * rate)
+def serving_streams(torch, seconds: float, rate: float):
+    """16 camera streams (8 QVGA, 8 VGA) of seconds * rate frames each, rendered
+    on the GPU: objects on bounded trajectories (reversing every 10 frames)."""
+    from pdflow import render_frames, scenes
+    T = int(seconds * rate) + 12
     streams = []
     for vga in (False, True):
         scs = [scenes.make_scene(8_000_000 + 100 * vga + j, vga, 3 + j % 4, period=10) for j in range(8)]
@@ -334,13 +338,44 @@ def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
                 w, h = sc.width, sc.height
                 ii = torch.empty((len(ks), h, w), dtype=torch.uint8, device="cuda")
                 zz = torch.empty((len(ks), h, w), dtype=torch.int16, device="cuda")
-                from pdflow import render_frames
                 render_frames(descs, ii.data_ptr(), zz.data_ptr(), None, torch.cuda.current_stream().cuda_stream)
                 ih, zh = ii.cpu().numpy(), zz.cpu().numpy().view(np.uint16)
                 frames += [(ih[q], zh[q]) for q in range(len(ks))]
             streams.append((sc.width, sc.height, frames))
+    return streams
+
+
+def serving_load(base, n: int, seconds: float, rate: float):
+    """n streams built from the 16 rendered ones (half QVGA, half VGA): stream
+    j replays base stream j % 16 from a frame offset of 3 * (j // 16), so
+    streams beyond 16 are independent cameras with the same statistics."""
+    T = int(seconds * rate)
+    qvga = [s for s in base if s[1] == 240]
+    vga = [s for s in base if s[1] == 480]
+    out = []
+    for j in range(n):
+        src = (qvga if j % 2 == 0 else vga)[(j // 2) % 8]
+        off = 3 * (j // 16)
+        out.append((src[0], src[1], src[2][off:off + T]))
+    return out
+
+
+def serving_run(torch, weights, iter_scale, margin, learned_main: bool, seconds=3.0, rate=30.0,
+                loads=(16, 32, 48, 64)):
+    """Camera streams (half QVGA, half VGA) at `rate` Hz with Poisson arrivals
+    through the request loop (8 streams per lane, so a lane batches up to 8
+    frames): a sweep over the number of streams with the headline
+    configuration's schedule, reporting per load point the offered and
+    delivered flows/s, the mean batch and p50/p99 latency, and the capacity
+    (the largest load whose p99 stays within one frame period and whose last
+    result arrives within one frame period of the last submission, i.e. no
+    backlog builds up); plus the 16-stream point with the other schedule for
+    comparison."""
+    from pdflow.serving import Server, simulate
+    base = serving_streams(torch, seconds, rate)
+
     def run(learned, streams_used):
-        srv = Server(device_budget_bytes=64 << 30, slots_per_lane=2, learned=learned,
+        srv = Server(device_budget_bytes=96 << 30, slots_per_lane=8, learned=learned,
                      iter_scale=iter_scale if learned else 1.0, energy_margin=margin,
                      net_params=weights if learned else None)
         with paused_gc():   # the load generator keeps its arrival schedule
@@ -351,16 +386,31 @@ def serving_run(torch, weights, iter_scale, margin, seconds=3.0, rate=30.0):
         srv.close()
         summary.update(vga_p50_ms=float(np.percentile(lat[480], 50)), vga_p99_ms=float(np.percentile(lat[480], 99)),
                        qvga_p50_ms=float(np.percentile(lat[240], 50)), qvga_p99_ms=float(np.percentile(lat[240], 99)),
-                       lanes=st["lanes"], batches=st["batches"], device_bytes=st["device_bytes"])
+                       lanes=st["lanes"], batches=st["batches"], device_bytes=st["device_bytes"],
+                       offered_flows_per_s=len(streams_used) * rate,
+                       learned=learned)
         return summary
 
-    summary = run(True, streams)
-    summary["streams_desc"] = ("8 QVGA rows=240 + 8 VGA rows=480, Poisson arrivals at 30 Hz each, "
-                               f"{seconds:.0f} s of frames, 2 streams per lane")
-    # the same request loop with the plain schedule (first half of the frames), for comparison
-    half = [(w, h, fr[:max(2, len(fr) // 2)]) for w, h, fr in streams]
-    plain = run(False, half)
-    summary["plain_schedule"] = {k: plain[k] for k in ("p50_ms", "p99_ms", "vga_p50_ms", "vga_p99_ms", "flows")}
+    points = []
+    for n in loads:
+        pt = run(learned_main, serving_load(base, n, seconds, rate))
+        pt["streams"] = n
+        points.append(pt)
+    period_ms = 1000.0 / rate
+    ok = [p for p in points if p["p99_ms"] is not None and p["p99_ms"] <= period_ms and p["drain_ms"] <= period_ms]
+    summary = dict(points[0])
+    summary["streams_desc"] = (f"{loads[0]} streams (half QVGA rows=240, half VGA rows=480), Poisson arrivals at "
+                               f"{rate:g} Hz each, {seconds:g} s of frames, 8 streams per lane; schedule: "
+                               + ("learned warm start" if learned_main else "plain"))
+    summary["load_sweep"] = [{k: p[k] for k in ("streams", "offered_flows_per_s", "flows_per_s", "mean_batch_pairs",
+                                                 "p50_ms", "p99_ms", "vga_p99_ms", "qvga_p99_ms", "lanes",
+                                                 "drain_ms", "arrival_lateness_p99_ms", "errors")} for p in points]
+    summary["capacity_flows_per_s"] = max((p["offered_flows_per_s"] for p in ok), default=None)
+    summary["capacity_rule"] = (f"largest offered load with p99 <= {period_ms:.1f} ms (one frame period) and the "
+                                f"last result within {period_ms:.1f} ms of the last submission")
+    other = run(not learned_main, serving_load(base, loads[0], seconds / 2, rate))
+    summary["other_schedule"] = {k: other[k] for k in ("learned", "p50_ms", "p99_ms", "vga_p50_ms", "vga_p99_ms",
+                                                       "flows", "mean_batch_pairs")}
     return summary
 
 
@@ -512,6 +562,7 @@ def ours(args):
             push()
             b.solve_learned(B, net, half, margin)
         b.synchronize()
+        ta, tb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ta.record(stream)
         fb_half = 0
         for _ in range(max(3, K // 2)):
@@ -536,20 +587,18 @@ def ours(args):
         _lib.check(lib.pdflow_time_level_iterations(b.handle, B, 5, iters, ctypes.byref(ms)), "level timing")
     alg_bytes = ALG_BYTES_PER_PX_ITER * B * R_f * C_f          # per iteration
     achieved = alg_bytes / (ms.value / iters / 1000.0) / 1e9
-    fine_form = tune[5]["form"] if len(tune) > 5 else 5
+    fine_form = tune[5]["form"] if len(tune) > 5 else 8
     fine_kk = tune[5]["iters_per_launch"] if len(tune) > 5 else 4
-    trf = profiled_traffic(fine_form)
-    traffic = None
-    if trf and trf.get("bytes_per_px_iter"):
-        # DRAM bytes per iteration, scaled from a 16-pair capture of the same
-        # level and form (traffic per pixel-iteration does not depend on the
-        # batch size: each launch reads the level's planes once)
-        traffic = float(trf["bytes_per_px_iter"]) * B * R_f * C_f
+    traffic = tile_traffic_per_iteration(fine_form, fine_kk, B * R_f * C_f)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": traffic, "traffic_basis": "DRAM bytes per iteration of the timed level (scaled ncu capture)",
+                "traffic": traffic,
+                "traffic_basis": "DRAM bytes per iteration of the timed level from the launch geometry of the "
+                                 "autotuned form: every plane of the level read once and the 13 state planes written "
+                                 "once per launch (halo re-reads are L2 hits), divided by the iterations per launch; "
+                                 "checked against ncu DRAM counters in profiles/",
                 "peak_kind": peak_kind,
-                "kernel": f"finest-level iterations (480x640, {B} pairs; k_iterate_tiles2, autotuned form "
-                          f"{fine_form}, {fine_kk} iterations per launch)",
+                "kernel": f"finest-level iterations (480x640, {B} pairs; {KERNEL_OF_FORM.get(fine_form, fine_form)}, "
+                          f"autotuned form {fine_form}, {fine_kk} iterations per launch)",
                 "algorithmic_bytes_per_px_iter": ALG_BYTES_PER_PX_ITER,
                 "ms_per_iteration": ms.value / iters}
 
@@ -684,9 +733,38 @@ def ours(args):
             sev[k][1].record(stream)
     torch.cuda.synchronize()
     single_ms = [a.elapsed_time(e) for a, e in sev]
-    s.freeGPUMemory()
     plain = {"pairs_s": 1000.0 / statistics.mean(single_ms), "p50_ms": statistics.median(single_ms),
              "p99_ms": float(np.quantile(single_ms, 0.99)), "steps": ns, "l2": "256 MB flush before each step"}
+
+    # ---------------- L2 side of the single pair ----------------
+    # A single pair's working set (~90 MB at VGA) lives in the 126 MB L2, so its
+    # iterations are bound by L2, not HBM: per level, algorithmic bytes of the
+    # iterations (one eager traced solve, L2 warm) against an L2 copy ceiling
+    # measured here by the library's own copy kernel (2 x 24 MiB, L2-resident).
+    l2_gbs = ctypes.c_float()
+    with torch.cuda.stream(stream):
+        _lib.check(lib.pdflow_measure_copy_gbs(24 << 20, 200, ctypes.c_void_p(stream.cuda_stream),
+                                               ctypes.byref(l2_gbs)), "L2 copy")
+        single_step()
+        tr1 = s.trace(1)
+    levels = []
+    alg_total, it_ms_total = 0.0, 0.0
+    for i, t in enumerate(tr1):
+        Ri, Ci, it = 15 << i, 20 << i, 100 - 15 * (len(tr1) - 1 - i)
+        alg = ALG_BYTES_PER_PX_ITER * Ri * Ci * it
+        alg_total += alg
+        it_ms_total += t["iterations_ms"]
+        gbs = alg / (t["iterations_ms"] / 1e3) / 1e9
+        levels.append({"level": f"{Ri}x{Ci}", "iterations_ms": round(t["iterations_ms"], 4),
+                       "iterations_alg_gbs": round(gbs, 1), "frac_of_l2": round(gbs / l2_gbs.value, 4)})
+    s.freeGPUMemory()
+    l2 = {"peak_gbs": l2_gbs.value, "peak_kind": "measured in this run (pdflow_measure_copy_gbs, 2 x 24 MiB float4 "
+                                                 "copy, 200 repetitions, L2-resident)",
+          "single_pair_levels": levels,
+          "single_pair_iterations_alg_gbs": alg_total / (it_ms_total / 1e3) / 1e9,
+          "single_pair_frac_of_l2": alg_total / (it_ms_total / 1e3) / 1e9 / l2_gbs.value,
+          "single_pair_frac_of_hbm": alg_total / (it_ms_total / 1e3) / 1e9 / hbm_peak}
+    roofline["l2"] = l2
 
     try:
         mixed = mixed_batch_run(torch)
@@ -696,24 +774,27 @@ def ours(args):
     serving = None
     if rank == 0 and args.serve_seconds > 0:
         try:
-            serving = serving_run(torch, weights, scale, margin, seconds=args.serve_seconds)
+            serving = serving_run(torch, weights, scale, margin, head["kind"] == "learned",
+                                  seconds=args.serve_seconds)
         except Exception as ex:
             serving = {"error": str(ex)}
 
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"VGA scene flow, rows=480 (640x480, 6 levels), learned warm start at 60x80 "
-                                   f"with {scale:g}x iterations and 1 % energy fallback, batch of {B} distinct pairs "
-                                   "per step", "rows": ROWS, "image": f"{WIDTH}x{HEIGHT}",
-                       "pairs_per_step_per_gpu": B, "parallelism": f"replicas x{ws}", "learned_warm_start": True,
+            "config": {"workload": f"VGA scene flow, rows=480 (640x480, 6 levels), batch of {B} distinct pairs per "
+                                   f"step; headline: {head['config']} (the fastest measured configuration within "
+                                   "1 mm mean EPE of the plain result)", "rows": ROWS, "image": f"{WIDTH}x{HEIGHT}",
+                       "pairs_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
+                       "learned_warm_start": head["kind"] == "learned",
                        "l2": "batch working set far above L2 (no flush); plain single pair: L2 flushed per step",
                        "scenes": "seeded plane + 1-8 rigidly moving boxes/spheres, rendered on the GPU"},
             "accuracy": accuracy,
             "batched": {"pairs_s": value, "step_ms": [round(x, 3) for x in step_ms],
                         "p50_ms_per_batch": statistics.median(step_ms),
                         "p99_ms_per_batch": float(np.quantile(step_ms, 0.99))},
-            "batched_plain": batched_plain, "plain_batch_trace": trace, "learned_half_iterations": learned_half,
+            "candidates": candidates, "learned": learned_rec,
+            "plain_batch_trace": trace, "learned_half_iterations": learned_half,
             "mixed_batch": mixed,
             "plain": plain,
             "speedup_vs_plain_single": value / plain["pairs_s"],
@@ -814,7 +895,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--iter-scale", type=float, default=0.75)
     ap.add_argument("--energy-margin", type=float, default=0.01)
-    ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--replica-selftest", action="store_true",
                     help="host-only check of the replica path (synthetic times over gloo)")
     args = ap.parse_args()

@@ -24,8 +24,16 @@ typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const flo
  * in CSF_cuda, pdflow_cudalib.h:71-122).  The final flow equals pdflow_solve's. */
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
-/* Selects how pdflow_solve runs a level's iterations: 5 (default) = every
- * level of a batch (more than one pair), and a single pair's levels above
+/* Selects how pdflow_solve runs a level's iterations: 8 (default) = every
+ * level of a batch (more than one pair), and a single pair's levels above 300
+ * pixels, as temporally blocked 24x24 tiles (halo 4, up to 4 iterations per
+ * launch) walked by one persistent CTA per SM, each tile's state and
+ * constants in registers (one pixel pair per thread, packed FP32x2) while
+ * the next tile's region streams into shared memory by two 4D TMA tensor
+ * copies; levels whose row count is not a multiple of 4 (15x20, 30x40) run
+ * form 5 there; 7 = the same tiles as one CTA per tile, four rows per
+ * thread with the state in registers and the constants in shared memory;
+ * 5 = every level of a batch, and a single pair's levels above
  * 300 pixels (all but 15x20), as temporally blocked shared-memory tiles (several
  * iterations per launch; 24x24 tiles, one pixel pair per thread in packed
  * FP32x2 arithmetic, two CTAs per SM so that one CTA's region load and store
@@ -87,6 +95,17 @@ int pdflow_set_tile_copy_mode(int shape, int mode);
  * prefetch per plane) the region of the CTA that many launch positions later,
  * which starts about when it finishes; 0 = no prefetch.  Same bits. */
 int pdflow_set_quad_prefetch(unsigned ctas_ahead);
+
+/* Copy bandwidth of this GPU for a working set of `bytes` per buffer (the
+ * roofline denominators; no counterpart in the reference): allocates two
+ * buffers of `bytes` and copies them into each other `reps` times within one
+ * launch (alternating directions; 16-byte loads and stores that bypass L1,
+ * 4 CTAs of 512 threads per SM, grid-stride) after a warm-up launch, timed
+ * with CUDA events on `stream`; returns read + written bytes per second in
+ * GB/s.  With 2 * bytes well inside L2 (e.g. 2 x 24 MiB on a 126 MB L2)
+ * every copy after the first is served by L2: the L2 bandwidth ceiling; with
+ * buffers far above L2 it is the HBM copy bandwidth. */
+int pdflow_measure_copy_gbs(size_t bytes, unsigned reps, void* stream, float* gbs);
 
 /* Per-level, per-phase timing of a plain solve of pairs [0, n) (tracing; no
  * counterpart in the reference, whose only timing is a host clock around the

@@ -238,6 +238,75 @@ int pdflow_time_level_iterations(pdflow_solver* s, unsigned n, unsigned level, u
     return e == cudaSuccess ? PDFLOW_OK : fail("timing", e);
 }
 
+}  // extern "C"
+
+namespace {
+
+// `passes` copies a -> b, b -> a, a -> b ... in one launch; each thread moves
+// the same elements every pass (no cross-thread hazard), with L2-level loads
+// and stores (ld/st.global.cg) that the compiler cannot fold across passes.
+__global__ void __launch_bounds__(512) k_copy4(float4* a, float4* b, size_t n, unsigned passes)
+{
+    for (unsigned r = 0; r < passes; ++r) {
+        float4* src = (r & 1) ? b : a;
+        float4* dst = (r & 1) ? a : b;
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+            float4 v;
+            asm volatile("ld.global.cg.v4.f32 {%0, %1, %2, %3}, [%4];"
+                         : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                         : "l"(src + i));
+            asm volatile("st.global.cg.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + i), "f"(v.x), "f"(v.y), "f"(v.z),
+                         "f"(v.w)
+                         : "memory");
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pdflow_measure_copy_gbs(size_t bytes, unsigned reps, void* stream, float* gbs)
+{
+    if (!gbs || bytes < 16 || reps == 0) return fail(PDFLOW_ERR_ARG, "bad size, repetitions or null output");
+    bytes &= ~size_t(15);
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail("device query", e);
+    void *a = nullptr, *b = nullptr;
+    if (cudaMalloc(&a, bytes) != cudaSuccess || cudaMalloc(&b, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        if (a) cudaFree(a);
+        return fail(PDFLOW_ERR_OOM, "copy buffers");
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t n = bytes / 16;
+    const unsigned grid = unsigned(sms) * 4u;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    e = cudaMemsetAsync(a, 0, bytes, st);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) {
+        k_copy4<<<grid, 512, 0, st>>>(static_cast<float4*>(a), static_cast<float4*>(b), n, 2);   // warm-up
+        e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) {
+            k_copy4<<<grid, 512, 0, st>>>(static_cast<float4*>(a), static_cast<float4*>(b), n, reps);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess) *gbs = float(2.0 * double(bytes) * reps / (double(ms) * 1e-3) / 1e9);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(a);
+    cudaFree(b);
+    return e == cudaSuccess ? PDFLOW_OK : fail("copy timing", e);
+}
+
 int pdflow_trace_solve(pdflow_solver* s, unsigned n, float* ms)
 {
     if (!s || !ms || n == 0 || n > s->batch) return fail(PDFLOW_ERR_ARG, "bad pair count or null output");

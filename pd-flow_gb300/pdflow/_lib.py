@@ -183,6 +183,7 @@ _SIGNATURES = {
     "pdflow_read_level_flow": (ctypes.c_int, [vp, u32, u32] + [vp] * 6),
     "pdflow_set_tile_copy_mode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "pdflow_set_quad_prefetch": (ctypes.c_int, [ctypes.c_uint]),
+    "pdflow_measure_copy_gbs": (ctypes.c_int, [ctypes.c_size_t, u32, vp, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_debug_wait_timeout": (ctypes.c_int, [vp, u32]),
     "pdflow_trace_solve": (ctypes.c_int, [vp, u32, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),
@@ -316,6 +317,17 @@ class _Extras:
               "pdflow_read_level_flow")
         return out
 
+    def trace(self, n: int):
+        """Per-level phase times of an eager plain solve of pairs [0, n)
+        (pdflow_trace_solve): [{setup_ms, iterations_ms, median_ms}] coarsest first."""
+        rows, cols, ctf = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+        check(load().pdflow_get_config(self.handle, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(ctf), None, None),
+              "pdflow_get_config")
+        ms = (ctypes.c_float * (3 * ctf.value))()
+        check(load().pdflow_trace_solve(self.handle, n, ms), "pdflow_trace_solve")
+        return [{"setup_ms": ms[3 * i], "iterations_ms": ms[3 * i + 1], "median_ms": ms[3 * i + 2]}
+                for i in range(ctf.value)]
+
     def pair_stride(self) -> int:
         cap, st = u32(), ctypes.c_size_t()
         check(load().pdflow_batch_info(self.handle, ctypes.byref(cap), ctypes.byref(st)), "pdflow_batch_info")
@@ -338,7 +350,7 @@ class Solver(_Extras):
     freeGPUMemory."""
 
     def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 5):
+                 use_graph: bool = True, iteration_form: int = 8):
         self.rows, self.width, self.height = rows, width, height
         self.cols = rows * 320 // 240
         self.params = params
@@ -483,7 +495,7 @@ class BatchSolver(_Extras):
     a camera stream that keeps its previous frame on the device."""
 
     def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 5):
+                 use_graph: bool = True, iteration_form: int = 8):
         lib = load()
         self.rows, self.width, self.height, self.max_pairs = rows, width, height, max_pairs
         self.cols = rows * 320 // 240
@@ -567,17 +579,6 @@ class BatchSolver(_Extras):
         return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
                  "ms_per_iter": [None if not np.isfinite(x) else float(x) for x in rep.level[i].ms_per_iter]}
                 for i in range(rep.levels)]
-
-    def trace(self, n: int):
-        """Per-level phase times of an eager plain solve of pairs [0, n)
-        (pdflow_trace_solve): [{setup_ms, iterations_ms, median_ms}] coarsest first."""
-        rows, cols, ctf = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
-        check(load().pdflow_get_config(self._h, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(ctf), None, None),
-              "pdflow_get_config")
-        ms = (ctypes.c_float * (3 * ctf.value))()
-        check(load().pdflow_trace_solve(self._h, n, ms), "pdflow_trace_solve")
-        return [{"setup_ms": ms[3 * i], "iterations_ms": ms[3 * i + 1], "median_ms": ms[3 * i + 2]}
-                for i in range(ctf.value)]
 
     def set_level_form(self, level: int, form: int, iters_per_launch: int = 0):
         check(load().pdflow_set_level_form(self._h, level, form, iters_per_launch), "pdflow_set_level_form")

@@ -126,6 +126,8 @@ def simulate(server: Server, streams, rate_hz: float = 30.0, seed: int = 0, want
                    mean_batch_pairs=float(np.mean([i["batch_pairs"] for i in infos if i["has_flow"]])) if flows else 0,
                    wall_s=wall, errors=int(sum(1 for i in infos if i["status"] != 0)),
                    arrival_lateness_p99_ms=float(np.percentile(late, 99)) if late else None,
+                   submit_span_ms=max(i["submit_ms"] for i in infos) - min(i["submit_ms"] for i in infos),
+                   drain_ms=max(i["done_ms"] for i in infos) - max(i["submit_ms"] for i in infos),
                    arrival_lateness_max_ms=float(max(late)) if late else None,
                    fallbacks=int(server.stats()["fallbacks"]))
     for sid in sids:
