@@ -217,14 +217,30 @@ def cpu_baseline(min_seconds: float = 10.0):
     oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")   # warm (page-in, OpenMP pool)
     n, t0 = 0, time.perf_counter()
     while True:
-        oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")
+        cpu = oracle.solve(ROWS, WIDTH, HEIGHT, I1, Z1, I2, Z2, precision="f32")
         n += 1
         dt = time.perf_counter() - t0
         if dt >= min_seconds:
             break
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": n / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
-            "sample": f"{n} VGA pairs (rows=480) solved by the FP32 OpenMP oracle in {dt:.1f} s"}
+    out = {"value": n / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
+           "sample": f"{n} VGA pairs (rows=480) solved by the FP32 OpenMP oracle in {dt:.1f} s"}
+    # agreement of the timed port with the GPU solver (bit-exact with the
+    # reference's CUDA build) on this pair: the port rounds every product
+    # separately where nvcc fuses, so near-tie branch flips of the non-smooth
+    # iteration move a few pixels by more than 1 mm
+    try:
+        from pdflow import Solver
+        s = Solver(ROWS, WIDTH, HEIGHT).initializeCUDA()
+        s.loadRGBDFrames(i1, z1, i2, z2)
+        s.solveSceneFlowGPU()
+        d = np.max([np.abs(a.astype(np.float64) - b) for a, b in zip((s.dxp, s.dyp, s.dzp), cpu)], axis=0)
+        s.freeGPUMemory()
+        out["vs_gpu"] = {"mean_abs_m": float(d.mean()), "max_abs_m": float(d.max()),
+                         "pixels_over_1mm": int((d > 1e-3).sum()), "pixels": int(d.size)}
+    except Exception as ex:  # reported, never required
+        out["vs_gpu"] = {"error": str(ex)}
+    return out
 
 
 def reference_arm(args):
