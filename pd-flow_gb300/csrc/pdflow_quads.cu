@@ -161,13 +161,15 @@ __device__ __forceinline__ Q shift_up(const Q& a, float below)
 
 __device__ __forceinline__ float clamp1(float pd) { return (fabsf(pd) > 1.f) ? ((pd > 1.f) ? 1.f : -1.f) : pd; }
 
+// Projection onto the unit disc (updateDualVariables, pdflow_cudalib.cu:813-887).
+// Branch-free: outside the projection the factor is 1 and x * 1 == x exactly,
+// so the bits are those of the reference's conditional update.
 __device__ __forceinline__ void disc(float& a, float& b)
 {
     const float m = rhypotf(a, b);
-    if (m < 1.f) {
-        a = mul(a, m);
-        b = mul(b, m);
-    }
+    const float f = (m < 1.f) ? m : 1.f;
+    a = mul(a, f);
+    b = mul(b, f);
 }
 
 // L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).

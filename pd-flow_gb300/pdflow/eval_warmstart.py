@@ -17,6 +17,11 @@ solve's, and the time of the batch:
              iterations scaled (the same iteration budget without a seed);
 * label_seed the scaled schedule from 60x80 seeded with the plain result
              itself averaged to 60x80 (what a perfect network would predict).
+
+`--schedules "25,40,55,70,85,95;..."` also solves the batch with plain
+schedules of other per-level iteration counts (coarsest level first) and
+reports their end-point error against the reference schedule's result and
+their time: how far a trajectory change moves the non-converged result.
 """
 from __future__ import annotations
 
@@ -114,6 +119,58 @@ def evaluate(weights, rows: int, pairs: int, scales, seed0: int = 3_000_000, mar
     return out
 
 
+def schedule_sweep(schedules, rows: int, pairs: int, seed0: int = 3_000_000, log=print):
+    """The plain batch under other per-level iteration counts, against the
+    reference schedule's result (same held-out pairs as `evaluate`)."""
+    import torch
+
+    from . import _lib
+    vga = rows == 480
+    w, h = (640, 480) if vga else (320, 240)
+    rng = np.random.default_rng(seed0)
+    seeds = list(range(seed0, seed0 + pairs))
+    nobj = {s: int(rng.integers(1, 9)) for s in seeds}
+    i1, z1, i2, z2, gt = datagen.render_pairs(torch, seeds, vga, n_objects=lambda s: nobj[s], with_flow=True)
+    valid = (z1.cpu().numpy().view(np.uint16) > 0).transpose(0, 2, 1).reshape(pairs, -1)
+    gt = gt.cpu().numpy()
+    gt = [gt[:, 0], gt[:, 1], gt[:, 2]]
+
+    def run(iters):
+        p = _lib.default_params(rows)
+        for k, v in enumerate(iters):
+            p.num_max_iter[k] = v
+        b = BatchSolver(rows, w, h, pairs, params=p)
+        b.push_raw_device(pairs, i1.data_ptr(), z1.data_ptr())
+        b.push_raw_device(pairs, i2.data_ptr(), z2.data_ptr())
+        b.autotune(pairs)
+        b.solve(pairs)
+        b.synchronize()
+        best = float("inf")
+        for _ in range(3):
+            t = time.perf_counter()
+            b.solve(pairs)
+            b.synchronize()
+            best = min(best, time.perf_counter() - t)
+        out = b.read_flow(pairs)
+        b.close()
+        return out, best
+
+    p0 = _lib.default_params(rows)
+    levels = (rows // 15).bit_length()
+    ref_iters = [p0.num_max_iter[k] for k in range(levels)]
+    ref, t0 = run(ref_iters)
+    res = [dict(schedule=ref_iters, ms=t0 * 1e3, epe_gt_mm=float(epe(ref, gt, valid).mean() * 1e3))]
+    log(json.dumps(res[0]))
+    for it in schedules:
+        out, t = run(it)
+        e = epe(out, ref, valid)
+        r = dict(schedule=it, ms=t * 1e3, speedup=t0 / t, epe_vs_plain_mm=float(e.mean() * 1e3),
+                 epe_vs_plain_max_pair_mm=float(e.max() * 1e3), epe_gt_mm=float(epe(out, gt, valid).mean() * 1e3))
+        res.append(r)
+        log(json.dumps(r))
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--weights", required=True)
@@ -121,7 +178,11 @@ def main():
     ap.add_argument("--pairs", type=int, default=64)
     ap.add_argument("--scales", default="0.5")
     ap.add_argument("--margin", type=float, default=0.01)
+    ap.add_argument("--schedules", default="",
+                    help="plain schedules to compare, e.g. \"25,40,55,70,85,95;25,40,55,70,43,100\"")
     a = ap.parse_args()
+    if a.schedules:
+        schedule_sweep([[int(x) for x in s.split(",")] for s in a.schedules.split(";") if s], a.rows, a.pairs)
     res = evaluate(load_weights(a.weights), a.rows, a.pairs, [float(x) for x in a.scales.split(",")],
                    margin=a.margin)
     print(json.dumps(res))
