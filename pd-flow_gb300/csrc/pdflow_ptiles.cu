@@ -85,20 +85,17 @@ __device__ __forceinline__ void disc(float& a, float& b)
     b = mul(b, f);
 }
 
-// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).
+// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).  All
+// three cases are evaluated and one is selected: a warp's lanes fall in
+// different cases, so the branches cost more than the two quotients (same
+// bits: each case's value is the reference's expression).
 __device__ __forceinline__ void shrink(float& du, float& dv, float of, float th, float a1, float b1)
 {
-    if (of < -th) {
-        du = add(du, a1);
-        dv = add(dv, b1);
-    } else if (of > th) {
-        du = sub(du, a1);
-        dv = sub(dv, b1);
-    } else {
-        const float den = add(th, 1e-10f);
-        du = sub(du, qt(mul(a1, of), den));
-        dv = sub(dv, qt(mul(b1, of), den));
-    }
+    const float den = add(th, 1e-10f);
+    const float mu_ = sub(du, qt(mul(a1, of), den)), mv_ = sub(dv, qt(mul(b1, of), den));
+    const bool lo = of < -th, hi = of > th;
+    du = lo ? add(du, a1) : (hi ? sub(du, a1) : mu_);
+    dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
 }
 
 struct Tile {
@@ -217,11 +214,15 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                 const float Vb = __shfl_down_sync(0xffffffffu, V.x, 1, 16);
                 const float Wb = __shfl_down_sync(0xffffffffu, wa.x, 1, 16);
                 __syncthreads();
-                float2 gu1 = zero, gv1 = zero, gw1 = zero;
-                if (!lu) {
-                    gu1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XU + right), U));
-                    gv1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XV + right), V));
-                    gw1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XW + right), wa));
+                // borders by selects, not branches (the neighbour slot at the
+                // region's right edge is the thread's own: read, then dropped)
+                float2 gu1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XU + right), U));
+                float2 gv1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XV + right), V));
+                float2 gw1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XW + right), wa));
+                if (lu) {
+                    gu1 = zero;
+                    gv1 = zero;
+                    gw1 = zero;
                 }
                 float2 gu2 = mul2(rj, sub2(make_float2(U.y, Ub), U));
                 float2 gv2 = mul2(rj, sub2(make_float2(V.y, Vb), V));
@@ -265,10 +266,9 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                 float2 div[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    float2 d;
-                    if (fu) d = mul2(ri, pu_[k]);
-                    else if (lu) d = neg2(*reinterpret_cast<const float2*>(Yp[k] + left));
-                    else d = fm2(ri, pu_[k], neg2(*reinterpret_cast<const float2*>(Yp[k] + left)));
+                    const float2 ym = neg2(*reinterpret_cast<const float2*>(Yp[k] + left));
+                    const float2 dm = fm2(ri, pu_[k], ym), df = mul2(ri, pu_[k]);
+                    float2 d = fu ? df : (lu ? ym : dm);   // first / last / inner column
                     float2 g = add2(d, fm2(rj, pv_[k], neg2(zm_[k])));
                     if (fv) g.x = fm(rj.x, pv_[k].x, d.x);
                     if (lv) g.y = fm(-rj.x, pv_[k].x, d.y);

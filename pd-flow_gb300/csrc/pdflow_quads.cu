@@ -172,20 +172,17 @@ __device__ __forceinline__ void disc(float& a, float& b)
     b = mul(b, f);
 }
 
-// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).
+// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).  All
+// three cases are evaluated and one is selected: a warp's lanes fall in
+// different cases, so the branches cost more than the two quotients (same
+// bits: each case's value is the reference's expression).
 __device__ __forceinline__ void shrink(float& du, float& dv, float of, float th, float a1, float b1)
 {
-    if (of < -th) {
-        du = add(du, a1);
-        dv = add(dv, b1);
-    } else if (of > th) {
-        du = sub(du, a1);
-        dv = sub(dv, b1);
-    } else {
-        const float den = add(th, 1e-10f);
-        du = sub(du, qt(mul(a1, of), den));
-        dv = sub(dv, qt(mul(b1, of), den));
-    }
+    const float den = add(th, 1e-10f);
+    const float mu_ = sub(du, qt(mul(a1, of), den)), mv_ = sub(dv, qt(mul(b1, of), den));
+    const bool lo = of < -th, hi = of > th;
+    du = lo ? add(du, a1) : (hi ? sub(du, a1) : mu_);
+    dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
 }
 
 __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, const __grid_constant__ QuadMaps tm)
@@ -301,11 +298,15 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
             const float Wb = __shfl_down_sync(0xffffffffu, wa.lo.x, 1, 8);
             __syncthreads();
             const Q ri = lds(P + C_RI * kQPlane + me), rj = lds(P + C_RJ * kQPlane + me);
-            Q gu1 = zero, gv1 = zero, gw1 = zero;
-            if (!lu) {
-                gu1 = qmul(ri, qsub(lds(XU + right), U));
-                gv1 = qmul(ri, qsub(lds(XV + right), V));
-                gw1 = qmul(ri, qsub(lds(XW + right), wa));
+            // borders by selects, not branches (the neighbour slot at the region's
+            // right edge is the thread's own: read, then dropped)
+            Q gu1 = qmul(ri, qsub(lds(XU + right), U));
+            Q gv1 = qmul(ri, qsub(lds(XV + right), V));
+            Q gw1 = qmul(ri, qsub(lds(XW + right), wa));
+            if (lu) {
+                gu1 = zero;
+                gv1 = zero;
+                gw1 = zero;
             }
             Q gu2 = qmul(rj, qsub(shift_up(U, Ub), U));
             Q gv2 = qmul(rj, qsub(shift_up(V, Vb), V));
@@ -361,10 +362,9 @@ __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, cons
             Q div[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                Q d;
-                if (fu) d = qmul(ri, pu_[k]);
-                else if (lu) d = qneg(lds(Yp[k] + left));
-                else d = qfm(ri, pu_[k], qneg(lds(Yp[k] + left)));
+                const Q ym = qneg(lds(Yp[k] + left));
+                const Q dm = qfm(ri, pu_[k], ym), df = qmul(ri, pu_[k]);
+                const Q d = fu ? df : (lu ? ym : dm);   // first / last / inner column
                 Q g = qadd(d, qfm(rj, pv_[k], qneg(z_[k])));
                 if (fv) g.lo.x = fm(rj.lo.x, pv_[k].lo.x, d.lo.x);
                 if (lv) g.hi.y = fm(-rj.hi.x, pv_[k].hi.x, d.hi.y);
