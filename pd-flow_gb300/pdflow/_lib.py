@@ -328,6 +328,18 @@ class _Extras:
         return [{"setup_ms": ms[3 * i], "iterations_ms": ms[3 * i + 1], "median_ms": ms[3 * i + 2]}
                 for i in range(ctf.value)]
 
+    def autotune(self, n: int, probe_iters: int = 12):
+        """Per-level launch form and iterations per launch for pairs [0, n)
+        (pdflow_autotune); returns [{form, iters_per_launch, ms_per_iter}] per level."""
+        rep = TuneReport()
+        check(load().pdflow_autotune(self.handle, n, probe_iters, ctypes.byref(rep)), "pdflow_autotune")
+        return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
+                 "ms_per_iter": [None if not np.isfinite(x) else float(x) for x in rep.level[i].ms_per_iter]}
+                for i in range(rep.levels)]
+
+    def set_level_form(self, level: int, form: int, iters_per_launch: int = 0):
+        check(load().pdflow_set_level_form(self.handle, level, form, iters_per_launch), "pdflow_set_level_form")
+
     def pair_stride(self) -> int:
         cap, st = u32(), ctypes.c_size_t()
         check(load().pdflow_batch_info(self.handle, ctypes.byref(cap), ctypes.byref(st)), "pdflow_batch_info")
@@ -570,18 +582,6 @@ class BatchSolver(_Extras):
         check(load().pdflow_read_flow_slots(self._h, len(sl), _ptr(sl), *[_ptr(a) for a in out]),
               "pdflow_read_flow_slots")
         return out
-
-    def autotune(self, n: int, probe_iters: int = 12):
-        """Per-level launch form and iterations per launch for pairs [0, n)
-        (pdflow_autotune); returns [{form, iters_per_launch, ms_per_iter}] per level."""
-        rep = TuneReport()
-        check(load().pdflow_autotune(self._h, n, probe_iters, ctypes.byref(rep)), "pdflow_autotune")
-        return [{"form": rep.level[i].form, "iters_per_launch": rep.level[i].iters_per_launch,
-                 "ms_per_iter": [None if not np.isfinite(x) else float(x) for x in rep.level[i].ms_per_iter]}
-                for i in range(rep.levels)]
-
-    def set_level_form(self, level: int, form: int, iters_per_launch: int = 0):
-        check(load().pdflow_set_level_form(self._h, level, form, iters_per_launch), "pdflow_set_level_form")
 
     def solve_learned(self, n: int, net: "Net", iter_scale: float = 0.5, energy_margin: float = 0.01):
         """Learned warm-start solve of pairs [0, n) (pdflow_solve_batch_learned)."""
