@@ -139,6 +139,14 @@ int enqueue_level_iterations(pdflow_solver* s, cudaStream_t st, unsigned pairs, 
 // Autotuner of a mixed-resolution handle (pdflow_mixed.cu): per coarse-to-fine
 // step, the tile form and iterations per launch over the pairs active there.
 int mixed_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_tune_report* report);
+
+// Candidate c (0 <= c < PDFLOW_TUNE_CANDIDATES) of the launch-form autotuners:
+// its iteration form and iterations per launch (0 for forms 0 and 1).
+struct TuneCandidate {
+    int form;
+    unsigned kk;
+};
+TuneCandidate tune_candidate(int c);
 int check_status(pdflow_solver* s);
 void set_last_error(const char* text);   // the text pdflow_last_error returns on this thread
 LevelGeom level_geom(const pdflow_solver* s, unsigned i, unsigned* level_image, unsigned pairs = 1);

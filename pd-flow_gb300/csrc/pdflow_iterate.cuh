@@ -61,14 +61,16 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
 // in L.qs, written by a kStepsQuads / kStepsAll set-up); same bits.  Needs
 // rows % 4 == 0 and 16-byte aligned planes (quads_eligible).
 cudaError_t prepare_quads();
-// Persistent streamed tiles (pdflow_ptiles.cu, iteration form 8): one CTA per
-// SM (`ctas` CTAs) walks every tile of the launch with its region in
-// registers while the next region streams into shared memory by TMA; same
-// preconditions (quads_eligible) and same bits.
+// Persistent streamed tiles (pdflow_ptiles.cu, iteration forms 8 and 9): one
+// CTA per SM (`ctas` CTAs) walks every 32x32 region of the launch with its
+// state in registers while the next region streams into shared memory by TMA;
+// halo 4 (24x24 interiors, form 8) or 8 (16x16 interiors, form 9, up to 8
+// iterations per launch); same preconditions (quads_eligible) and same bits.
 cudaError_t prepare_stream_tiles();
 size_t stream_smem_bytes();
 cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
-                                  unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas);
+                                  unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas,
+                                  unsigned halo = 4);
 // L2 prefetch distance of the quad tiles in CTAs (0 = off).
 void set_quad_prefetch(unsigned ctas_ahead);
 size_t quads_smem_bytes();

@@ -44,15 +44,16 @@ struct LaunchRec {
     unsigned step, kk, off, count;
 };
 
-// Iterations per tile launch at step i (the autotuned choice, else 4).
-unsigned step_kk(const pdflow_solver* s, unsigned i)
+// Iterations per tile launch at step i in form `form` (the autotuned choice,
+// else the halo width: 8 for the deep streamed tiles of form 9, else 4).
+unsigned step_kk(const pdflow_solver* s, unsigned i, int form)
 {
-    const unsigned k = s->mixed_kk[i];
-    return (k >= 1 && k <= 4) ? k : 4u;
+    const unsigned k = s->mixed_kk[i], h = form == 9 ? 8u : 4u;
+    return (k >= 1 && k <= h) ? k : h;
 }
 
 // Tile form at step i: the autotuned choice, else the handle's paired form
-// (forms 7 and 8 need rows % 4 == 0, levels 15x20 and 30x40 run form 5).
+// (forms 7-9 need rows % 4 == 0, levels 15x20 and 30x40 run form 5).
 int step_form(const pdflow_solver* s, unsigned i, const LevelGeom& g)
 {
     int f = s->mixed_form[i] >= 3 ? s->mixed_form[i] : (s->iter_form >= 3 ? s->iter_form : 5);
@@ -75,7 +76,9 @@ LevelGeom step_geom(const pdflow_solver* s, unsigned step, unsigned pairs, const
 cudaError_t launch_step_tiles(pdflow_solver* s, const LevelGeom& g, const State& cur, const State& nxt,
                               const Params& p, const PyrLevel& o, unsigned kk, cudaStream_t st, int form)
 {
-    if (form == 8) return launch_iterate_stream(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status, s->num_sms);
+    if (form >= 8)
+        return launch_iterate_stream(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status, s->num_sms,
+                                     form == 9 ? 8u : 4u);
     if (form == 7) return launch_iterate_quads(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status);
     return launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, false, st, form - 3, s->status);
 }
@@ -96,8 +99,9 @@ void build_plan(const pdflow_solver* s, const std::vector<unsigned>& rows, std::
         table.insert(table.end(), act.begin(), act.end());
         std::vector<unsigned> remaining(act.size()), launches(act.size(), 0);
         for (size_t a = 0; a < act.size(); ++a) remaining[a] = 100u - 15u * (levels_of(rows[act[a]]) - 1u - i);
+        const unsigned step_k = step_kk(s, i, step_form(s, i, step_geom(s, i, unsigned(act.size()), nullptr)));
         for (;;) {
-            unsigned kk = step_kk(s, i), live = 0;
+            unsigned kk = step_k, live = 0;
             for (unsigned r : remaining)
                 if (r > 0) {
                     kk = std::min(kk, r);
@@ -127,9 +131,10 @@ int prepare_plan(pdflow_solver* s, const std::vector<unsigned>& rows, std::vecto
     build_plan(s, rows, plan, table);
     std::vector<unsigned> sig(rows);
     for (unsigned i = 0; i < kSteps; ++i) {
-        sig.push_back(step_kk(s, i));
+        sig.push_back(s->mixed_kk[i]);
         sig.push_back(unsigned(s->mixed_form[i] + 1));
     }
+    sig.push_back(unsigned(s->iter_form + 1));   // the default iterations per launch follow the form
     if (sig == s->plan_rows) return PDFLOW_OK;
     if (table.size() > s->map_table_cap) {
         if (s->map_table) cudaFree(s->map_table);
@@ -232,11 +237,9 @@ int pdflow::mixed_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, p
         float best = INFINITY;
         int best_form = 5;
         unsigned best_kk = 4;
-        int c = 0;
-        for (int form = 0; form <= 8; ++form)
-            for (unsigned kk : {0u, 2u, 3u, 4u}) {
-                if ((form <= 1) != (kk == 0)) continue;   // the candidate list of pdflow_tune.cu
-                const int idx = c++;
+        for (int idx = 0; idx < PDFLOW_TUNE_CANDIDATES; ++idx) {
+                const int form = tune_candidate(idx).form;
+                const unsigned kk = tune_candidate(idx).kk;
                 if (form < 3) continue;                   // mixed steps run tile forms only
                 if (form >= 7 && !quads_eligible(g, s->L, s->S, s->S)) continue;
                 float t = INFINITY;

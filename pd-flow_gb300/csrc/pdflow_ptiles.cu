@@ -36,9 +36,10 @@ namespace {
 
 using namespace pack;
 
-constexpr int kSH = 4;                         // halo (iterations per launch at most)
-constexpr int kST = 24;                        // interior rows and columns
-constexpr int kSR = kST + 2 * kSH;             // region rows and columns (32)
+constexpr int kSR = 32;                        // region rows and columns
+// Interior and halo (= iterations per launch at most) are launch parameters:
+// 24 + 2 x 4 (form 8) or 16 + 2 x 8 (form 9: twice the iterations per launch
+// for levels whose launches are latency-bound, at four times the halo work).
 constexpr int kSPlane = kSR * kSR;             // floats per shared plane
 constexpr int kSThreads = kSR * kSR / 2;       // one thread per pixel pair (512)
 
@@ -57,6 +58,7 @@ struct StreamArgs {
     Params p;
     unsigned kk;
     bool last;
+    int tile, halo;            // interior rows and columns, halo width (tile + 2 halo = kSR)
     unsigned tiles_v;          // tiles per column of tiles
     unsigned tiles;            // tiles per pair
     unsigned total;            // tiles of the launch (tiles * pairs)
@@ -110,12 +112,12 @@ __device__ __forceinline__ Tile tile_at(const StreamArgs& a, unsigned n)
     const unsigned x = n % a.tiles;
     const int R = (int)a.g.R, C = (int)a.g.C;
     const int tv = (int)(x % a.tiles_v), tu = (int)(x / a.tiles_v);
-    t.iv0 = tv * kST;
-    t.iu0 = tu * kST;
-    t.iv1 = min(t.iv0 + kST, R);
-    t.iu1 = min(t.iu0 + kST, C);
-    t.rv0 = max(t.iv0 - kSH, 0);
-    t.ru0 = max(t.iu0 - kSH, 0);
+    t.iv0 = tv * a.tile;
+    t.iu0 = tu * a.tile;
+    t.iv1 = min(t.iv0 + a.tile, R);
+    t.iu1 = min(t.iu0 + a.tile, C);
+    t.rv0 = max(t.iv0 - a.halo, 0);
+    t.ru0 = max(t.iu0 - a.halo, 0);
     return t;
 }
 
@@ -327,8 +329,13 @@ cudaError_t prepare_stream_tiles()
 }
 
 cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
-                                  unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas)
+                                  unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas,
+                                  unsigned halo)
 {
+    // the region stays 32 x 32; rows of region origins stay multiples of 4
+    // (16-byte tensor-copy coordinates): halo 4 (interior 24) or 8 (interior 16)
+    if (halo != 4 && halo != 8) return cudaErrorInvalidValue;
+    const int kSH = int(halo), kST = kSR - 2 * int(halo);
     // same preconditions as the quad tiles (16-byte aligned planes, rows % 4 == 0)
     if (kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0)
         return cudaErrorInvalidValue;
@@ -342,6 +349,8 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     a.kk = kk;
     a.last = last;
     a.status = status;
+    a.tile = kST;
+    a.halo = kSH;
     a.tiles_v = (g.R + kST - 1) / kST;
     a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
     a.total = a.tiles * g.pairs;

@@ -32,7 +32,7 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
-TUNE_CANDIDATES = 23   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..8 x {2, 3, 4} iterations per launch
+TUNE_CANDIDATES = 26   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..8 x {2, 3, 4}, form 9 x {4, 6, 8}
 
 
 class TuneLevel(ctypes.Structure):
