@@ -294,13 +294,13 @@ def measured_peaks():
 # SMs, per iteration form: every launch reads each plane of the level once
 # (the halo's re-reads are L2 hits) and writes the 13 state planes once.
 #   forms 3-6 (shared-memory tiles): 13 state + 11 constants in, 13 out;
-#   forms 7-9 (register tiles): 13 state + 19 constants (the 8 step products
+#   forms 7-10 (register tiles): 13 state + 19 constants (the 8 step products
 #   are loaded, not recomputed) in, 13 out.
-TILE_FLOATS_IN = {3: 24, 4: 24, 5: 24, 6: 24, 7: 32, 8: 32, 9: 32}
+TILE_FLOATS_IN = {3: 24, 4: 24, 5: 24, 6: 24, 7: 32, 8: 32, 9: 32, 10: 32}
 TILE_FLOATS_OUT = 13
 KERNEL_OF_FORM = {3: "k_iterate_tiles2<40,40>", 4: "k_iterate_tiles2<40,34>", 5: "k_iterate_tiles2<24,24>",
                   6: "k_iterate_tiles2<24,28>", 7: "k_iterate_quads", 8: "k_iterate_stream",
-                  9: "k_iterate_stream (16x16 interiors)"}
+                  9: "k_iterate_stream (16x16 interiors)", 10: "k_iterate_stream (strips)"}
 
 
 def tile_traffic_per_iteration(form: int, kk: int, pixels: int):

@@ -234,7 +234,9 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * walked by one persistent CTA per SM with the state and constants in
  * registers while the next region streams into shared memory by TMA, levels
  * with rows % 4 == 0; form 9: the same with 16x16 interiors and a halo of 8,
- * up to 8 iterations per launch, for levels whose launches are latency-bound).
+ * up to 8 iterations per launch, for levels whose launches are latency-bound;
+ * form 10: rows of regions walked left to right, each handing the next its
+ * last exact column's exchange values, so no left halo is recomputed).
  * pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The
@@ -243,10 +245,10 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * step (report level i = the 15*2^i x 20*2^i step) over the pairs active at
  * that step, among the tile forms 3..8 (2, 3 or 4 iterations per launch);
  * pdflow_solve_mixed then runs each step in its chosen form. */
-#define PDFLOW_TUNE_CANDIDATES 26     /* form 0, form 1, forms 2..8 x {2, 3, 4}, form 9 x {4, 6, 8} iterations per launch */
+#define PDFLOW_TUNE_CANDIDATES 29     /* form 0, form 1, forms 2..8 x {2, 3, 4}, form 9 x {4, 6, 8}, form 10 x {2, 3, 4} */
 typedef struct pdflow_tune_level {
     int form;                         /* chosen form */
-    unsigned iters_per_launch;        /* chosen iterations per launch (forms 2..9) */
+    unsigned iters_per_launch;        /* chosen iterations per launch (forms 2..10) */
     float ms_per_iter[PDFLOW_TUNE_CANDIDATES];   /* per candidate; NaN if not eligible */
 } pdflow_tune_level;
 typedef struct pdflow_tune_report {

@@ -200,7 +200,7 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx)
 
 int pdflow_set_iteration_form(pdflow_solver* s, int form)
 {
-    if (!s || form < 0 || form > 9) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..9");
+    if (!s || form < 0 || form > 10) return fail(PDFLOW_ERR_ARG, "iteration form must be 0..10");
     if (s->iter_form != form) {
         cudaStreamSynchronize(s->stream);
         s->iter_form = form;   // graphs are cached per iteration form

@@ -61,16 +61,24 @@ cudaError_t launch_iterate_tiles2(LevelGeom g, LevelConsts L, State src, State d
 // in L.qs, written by a kStepsQuads / kStepsAll set-up); same bits.  Needs
 // rows % 4 == 0 and 16-byte aligned planes (quads_eligible).
 cudaError_t prepare_quads();
-// Persistent streamed tiles (pdflow_ptiles.cu, iteration forms 8 and 9): one
-// CTA per SM (`ctas` CTAs) walks every 32x32 region of the launch with its
-// state in registers while the next region streams into shared memory by TMA;
-// halo 4 (24x24 interiors, form 8) or 8 (16x16 interiors, form 9, up to 8
-// iterations per launch); same preconditions (quads_eligible) and same bits.
+// Persistent streamed tiles (pdflow_ptiles.cu, iteration forms 8-10): one
+// CTA per SM (`ctas` CTAs) walks 32x32 regions of the launch with their
+// state in registers while the next region streams into shared memory by
+// TMA: 24x24 interiors and a halo of 4 (form 8), 16x16 interiors and a halo
+// of 8 (form 9, up to 8 iterations per launch), or rows of regions walked
+// left to right that carry their left neighbour's exchange values (form 10,
+// 24-row interiors, 32 - kk exact columns per region); same preconditions
+// (quads_eligible) and same bits.
+enum class StreamLayout { Tiles24, Tiles16, Strips };
+inline StreamLayout stream_layout(int form)
+{
+    return form == 9 ? StreamLayout::Tiles16 : (form == 10 ? StreamLayout::Strips : StreamLayout::Tiles24);
+}
 cudaError_t prepare_stream_tiles();
 size_t stream_smem_bytes();
 cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
                                   unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas,
-                                  unsigned halo = 4);
+                                  StreamLayout layout);
 // L2 prefetch distance of the quad tiles in CTAs (0 = off).
 void set_quad_prefetch(unsigned ctas_ahead);
 size_t quads_smem_bytes();

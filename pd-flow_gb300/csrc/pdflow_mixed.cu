@@ -53,7 +53,7 @@ unsigned step_kk(const pdflow_solver* s, unsigned i, int form)
 }
 
 // Tile form at step i: the autotuned choice, else the handle's paired form
-// (forms 7-9 need rows % 4 == 0, levels 15x20 and 30x40 run form 5).
+// (forms 7-10 need rows % 4 == 0, levels 15x20 and 30x40 run form 5).
 int step_form(const pdflow_solver* s, unsigned i, const LevelGeom& g)
 {
     int f = s->mixed_form[i] >= 3 ? s->mixed_form[i] : (s->iter_form >= 3 ? s->iter_form : 5);
@@ -78,7 +78,7 @@ cudaError_t launch_step_tiles(pdflow_solver* s, const LevelGeom& g, const State&
 {
     if (form >= 8)
         return launch_iterate_stream(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status, s->num_sms,
-                                     form == 9 ? 8u : 4u);
+                                     stream_layout(form));
     if (form == 7) return launch_iterate_quads(g, s->L, cur, nxt, p, o.dep, kk, false, st, s->status);
     return launch_iterate_tiles2(g, s->L, cur, nxt, p, o.dep, kk, false, st, form - 3, s->status);
 }

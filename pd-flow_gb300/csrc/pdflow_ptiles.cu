@@ -23,7 +23,23 @@
 // the region is updated in every iteration; the stale ring at non-border
 // region edges is never read by an exact pixel and only the interior is
 // stored.  Needs rows % 4 == 0 (16-byte aligned tensor-copy rows).
+//
+// Strips (iteration form 10).  Of an iteration's column neighbours only the
+// primal step's backward difference looks left (ri * the dual's u-component
+// at column u - 1), and only the dual step's forward difference looks right.
+// A CTA that walks a row of regions left to right can therefore hand the
+// next region the left neighbour's exchange values of every iteration (a
+// carry of 3 x 32 floats per iteration, in shared memory) instead of
+// recomputing a left halo: after kk iterations columns [x, x + 32 - kk) of a
+// region at column x are exact, 28 of 32 at kk = 4 instead of 24.  The
+// strips (a pair's 24-row bands) are dealt round-robin, so that the CTAs walk
+// vertically adjacent bands side by side (their row halos meet in L2 and
+// their reads fill DRAM pages, as the tiles' do); the strips of a last,
+// partial round are cut into column pieces, one per idle CTA, each starting
+// with a region that recomputes a left halo of kk columns.
 #include <cuda.h>
+
+#include <algorithm>
 
 #include "pdflow_iterate.cuh"
 #include "pdflow_math.cuh"
@@ -53,6 +69,8 @@ enum { S_DU, S_DV, S_DW, S_UA, S_VA, S_WA, S_PD, S_PUU, S_PUV, S_PVU, S_PVV, S_P
 
 struct StreamArgs {
     LevelGeom g;
+    unsigned strips;           // strips: pairs x tiles_v
+    unsigned pieces;           // strips: pieces per strip of the last, partial round
     float* dst[13];            // du dv dw du_acc dv_acc dw_acc pd puu puv pvu pvv pwu pwv (interior written)
     const float* depth_old;
     Params p;
@@ -87,6 +105,18 @@ __device__ __forceinline__ void disc(float& a, float& b)
     b = mul(b, f);
 }
 
+// Both pixels of a pair.  Inside the disc of radius sqrt(0.999) rhypotf
+// (maximum error 2 ulp) returns more than 1, the factor is 1 and the values
+// stay as they are: a warp whose 64 pixels are all there skips the
+// reciprocal norms (NaN and infinite inputs fail the test and take them).
+__device__ __forceinline__ void disc2(float2& a, float2& b)
+{
+    const float2 s = fm2(a, a, mul2(b, b));
+    if (__all_sync(0xffffffffu, s.x < 0.999f && s.y < 0.999f)) return;
+    disc(a.x, b.x);
+    disc(a.y, b.y);
+}
+
 // L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).  All
 // three cases are evaluated and one is selected: a warp's lanes fall in
 // different cases, so the branches cost more than the two quotients (same
@@ -100,14 +130,25 @@ __device__ __forceinline__ void shrink(float& du, float& dv, float of, float th,
     dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
 }
 
+// One region of a CTA's walk: its origin, the rows and columns it stores,
+// and (strips) where the walk goes next.
 struct Tile {
-    unsigned y;                // grid pair index
+    unsigned y;                  // grid pair index
     int rv0, ru0, iv0, iv1, iu0, iu1;
+    bool more;                   // a region to process
+    bool carry_in, carry_out;    // strips: reads / writes the column carry
+    unsigned k;                  // strips: the CTA's segment; tiles: the tile index
+    int c1;                      // strips: the segment's end column
 };
 
+// Tiles: the launch's tile n (regions of every pair, dealt round-robin).
 __device__ __forceinline__ Tile tile_at(const StreamArgs& a, unsigned n)
 {
     Tile t;
+    t.more = n < a.total;
+    t.k = n;
+    t.c1 = 0;
+    t.carry_in = t.carry_out = false;
     t.y = n / a.tiles;
     const unsigned x = n % a.tiles;
     const int R = (int)a.g.R, C = (int)a.g.C;
@@ -121,12 +162,69 @@ __device__ __forceinline__ Tile tile_at(const StreamArgs& a, unsigned n)
     return t;
 }
 
-// Thread 0: the tensor copies of tile n's region into the staging planes,
+// Strips: segment k of this CTA's walk, columns [c0, c1) of strip `strip`
+// (strip s is row band s % tiles_v of pair s / tiles_v).  Full rounds: strip
+// k * G + b, all columns; the last round's r strips: piece b / r of strip
+// F * G + b % r.
+struct Segment {
+    bool ok;
+    unsigned strip;
+    int c0, c1;
+};
+__device__ __forceinline__ Segment segment(const StreamArgs& a, unsigned k)
+{
+    const unsigned G = gridDim.x, b = blockIdx.x, F = a.strips / G, r = a.strips - F * G;
+    const int C = (int)a.g.C;
+    if (k < F) return {true, k * G + b, 0, C};
+    if (k == F && b < r * a.pieces) {
+        const int i = (int)(b / r), n = (int)a.pieces;
+        return {true, F * G + b % r, C * i / n, C * (i + 1) / n};
+    }
+    return {false, 0, 0, 0};
+}
+
+// Strips: the region of segment k whose stored columns start at `col`.  With
+// the carry the region starts at that column; without it, kk columns further
+// left (their values go stale from the left, one column per iteration) or at
+// the image's first column.  Columns up to 32 - kk past the origin are exact
+// (all of them when the region reaches the image's last column).
+__device__ __forceinline__ Tile strip_at(const StreamArgs& a, unsigned k, int col, bool carry)
+{
+    Tile t;
+    const Segment sg = segment(a, k);
+    t.more = sg.ok;
+    t.k = k;
+    t.c1 = sg.c1;
+    const int R = (int)a.g.R, C = (int)a.g.C, K = (int)a.kk;
+    if (col < 0) col = sg.c0;
+    t.y = sg.strip / a.tiles_v;
+    const int tv = (int)(sg.strip - t.y * a.tiles_v);
+    t.iv0 = tv * a.tile;
+    t.iv1 = min(t.iv0 + a.tile, R);
+    t.rv0 = max(t.iv0 - a.halo, 0);
+    t.ru0 = carry ? col : max(col - K, 0);
+    const int exact = (t.ru0 + kSR >= C) ? C : t.ru0 + kSR - K;
+    t.iu0 = col;
+    t.iu1 = min(exact, sg.c1);
+    t.carry_in = carry;
+    t.carry_out = t.iu1 == exact && t.iu1 < sg.c1;   // the next region continues the segment
+    return t;
+}
+
+template <bool kStrips>
+__device__ __forceinline__ Tile next_tile(const StreamArgs& a, const Tile& t)
+{
+    if constexpr (kStrips)
+        return t.iu1 < t.c1 ? strip_at(a, t.k, t.iu1, true) : strip_at(a, t.k + 1, -1, false);
+    else
+        return tile_at(a, t.k + gridDim.x);
+}
+
+// Thread 0: the tensor copies of region t into the staging planes,
 // completing on `bar` (the caller's threads have finished reading staging).
 __device__ __forceinline__ void issue_region(const StreamArgs& a, const StreamMaps& tm, float* sm, uint32_t bar,
-                                             unsigned n)
+                                             const Tile& t)
 {
-    const Tile t = tile_at(a, n);
     const int slot = (int)(a.g.map ? (__ldg(a.g.map + t.y) & kMapSlotMask) : t.y);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // earlier generic reads before async writes
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
@@ -144,6 +242,11 @@ __device__ __forceinline__ void issue_region(const StreamArgs& a, const StreamMa
         : "memory");
 }
 
+// carry (strips): [buffer][iteration][u, v, w][region row] of the column
+// that the next region of the strip sees on its left
+constexpr int kCarryFloats = 2 * 4 * 3 * kSR;
+
+template <bool kStrips>
 __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, const __grid_constant__ StreamMaps tm)
 {
     extern __shared__ __align__(128) float sm[];
@@ -166,15 +269,22 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
     float* YW = sm + Y_W * kSPlane;
     auto ld2s = [&](int plane) { return *reinterpret_cast<const float2*>(sm + plane * kSPlane + me); };
 
+    float* carry = sm + N_PLANES * kSPlane;
+    const int cc = kSR - 1 - (int)a.kk;              // strips: the column the next region needs
+    // this CTA's walk: tiles blockIdx.x, + gridDim.x, ...; or its strip segments
+    Tile tl;
+    if constexpr (kStrips)
+        tl = strip_at(a, 0, -1, false);
+    else
+        tl = tile_at(a, blockIdx.x);
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if (blockIdx.x < a.total) issue_region(a, tm, sm, bar, blockIdx.x);
+        if (tl.more) issue_region(a, tm, sm, bar, tl);
     }
     __syncthreads();   // the mbarrier's initialisation before anyone waits on it
     uint32_t phase = 0;
-    for (unsigned n = blockIdx.x; n < a.total; n += gridDim.x) {
-        const Tile tl = tile_at(a, n);
+    for (unsigned n = 0; tl.more; ++n) {
         const size_t po = pair_off(a.g.map, a.g.pstride, tl.y);
         const int u = tl.ru0 + c, v0 = tl.rv0 + 2 * p;
         const bool live = u < C && v0 < R;           // v0 < R implies v0 + 1 < R (R even)
@@ -200,7 +310,18 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
             return;
         }
         phase ^= 1u;
-        if (t == 0 && n + gridDim.x < a.total) issue_region(a, tm, sm, bar, n + gridDim.x);
+        if (t == 0) {
+            const Tile nx = next_tile<kStrips>(a, tl);
+            if (nx.more) issue_region(a, tm, sm, bar, nx);
+        }
+        // the left neighbour's exchange values: the carry of the previous
+        // region (strips, first column) or the exchange planes; j advances
+        // the carry by one iteration
+        const bool from_carry = kStrips && tl.carry_in && c == 0;
+        const float* yl = from_carry ? carry + ((n + 1) & 1) * (4 * 3 * kSR) + 2 * p : sm + Y_U * kSPlane + left;
+        const int yl_k = from_carry ? kSR : kSPlane, yl_j = from_carry ? 3 * kSR : 0;
+        float* yc = carry + (n & 1) * (4 * 3 * kSR) + 2 * p;
+        const bool to_carry = kStrips && tl.carry_out && c == cc;
 
         const float2 mudu = mul2(mu, ddu), mudv = mul2(mu, ddv);
         const float2 a1 = mul2(tu, dcu), b1 = mul2(tv, dcv);
@@ -244,12 +365,9 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                 pwv = fm2(s4, gw2, pwv);
                 pd.x = clamp1(pd.x);
                 pd.y = clamp1(pd.y);
-                disc(puu.x, puv.x);
-                disc(puu.y, puv.y);
-                disc(pvu.x, pvv.x);
-                disc(pvu.y, pvv.y);
-                disc(pwu.x, pwv.x);
-                disc(pwu.y, pwv.y);
+                disc2(puu, puv);
+                disc2(pvu, pvv);
+                disc2(pwu, pwv);
             }
             // ---------------- primal step (computeDivergence + updatePrimalVariables) ----------------
             {
@@ -257,6 +375,12 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                 *reinterpret_cast<float2*>(YU + me) = yu;
                 *reinterpret_cast<float2*>(YV + me) = yv;
                 *reinterpret_cast<float2*>(YW + me) = yw;
+                if (to_carry) {
+                    float* y = yc + j * (3 * kSR);
+                    *reinterpret_cast<float2*>(y) = yu;
+                    *reinterpret_cast<float2*>(y + kSR) = yv;
+                    *reinterpret_cast<float2*>(y + 2 * kSR) = yw;
+                }
                 const float2 zu = mul2(rj, puv), zv = mul2(rj, pvv), zw = mul2(rj, pwv);
                 const float zua = __shfl_up_sync(0xffffffffu, zu.y, 1, 16);   // the previous pair's second row
                 const float zva = __shfl_up_sync(0xffffffffu, zv.y, 1, 16);
@@ -264,11 +388,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                 __syncthreads();
                 const float2 pu_[3] = {puu, pvu, pwu}, pv_[3] = {puv, pvv, pwv};
                 const float2 zm_[3] = {make_float2(zua, zu.x), make_float2(zva, zv.x), make_float2(zwa, zw.x)};
-                const float* Yp[3] = {YU, YV, YW};
                 float2 div[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const float2 ym = neg2(*reinterpret_cast<const float2*>(Yp[k] + left));
+                    const float2 ym = neg2(*reinterpret_cast<const float2*>(yl + k * yl_k + (int)j * yl_j));
                     const float2 dm = fm2(ri, pu_[k], ym), df = mul2(ri, pu_[k]);
                     float2 d = fu ? df : (lu ? ym : dm);   // first / last / inner column
                     float2 g = add2(d, fm2(rj, pv_[k], neg2(zm_[k])));
@@ -311,33 +434,36 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
             for (int k = 0; k < 13; ++k) *reinterpret_cast<float2*>(at(a.dst[k], po) + gi) = st[k];
         }
         // the next tile's staging wait is followed by a barrier before its first
-        // exchange store, so the exchange planes need none here
+        // exchange store, so the exchange planes (and the carry) need none here
+        tl = next_tile<kStrips>(a, tl);
     }
 }
 
 }  // namespace
 
-size_t stream_smem_bytes() { return sizeof(float) * N_PLANES * kSPlane; }
+size_t stream_smem_bytes() { return sizeof(float) * (N_PLANES * kSPlane + kCarryFloats); }
 
 cudaError_t prepare_stream_tiles()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_iterate_stream, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)stream_smem_bytes());
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_iterate_stream, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaError_t e = cudaSuccess;
+    for (const void* k : {(const void*)k_iterate_stream<false>, (const void*)k_iterate_stream<true>}) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stream_smem_bytes());
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    }
     return e;
 }
 
 cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State dst, Params p, const float* depth_old,
                                   unsigned kk, bool last, cudaStream_t st, unsigned* status, unsigned ctas,
-                                  unsigned halo)
+                                  StreamLayout layout)
 {
     // the region stays 32 x 32; rows of region origins stay multiples of 4
     // (16-byte tensor-copy coordinates): halo 4 (interior 24) or 8 (interior 16)
-    if (halo != 4 && halo != 8) return cudaErrorInvalidValue;
-    const int kSH = int(halo), kST = kSR - 2 * int(halo);
+    const bool strips = layout == StreamLayout::Strips;
+    const int kSH = layout == StreamLayout::Tiles16 ? 8 : 4, kST = kSR - 2 * kSH;
     // same preconditions as the quad tiles (16-byte aligned planes, rows % 4 == 0)
-    if (kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0)
+    if (kk == 0 || kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0)
         return cudaErrorInvalidValue;
     StreamArgs a;
     a.g = g;
@@ -354,6 +480,12 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     a.tiles_v = (g.R + kST - 1) / kST;
     a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
     a.total = a.tiles * g.pairs;
+    a.strips = g.pairs * a.tiles_v;
+    const unsigned grid = ctas < a.total ? ctas : a.total;
+    // pieces of the last round's strips: one per idle CTA, at least 32 - 2 kk
+    // exact columns each
+    const unsigned rest = a.strips % grid, most = (g.C + (kSR - 2 * kk) - 1) / (kSR - 2 * kk);
+    a.pieces = rest ? std::max(1u, std::min(grid / rest, most)) : 1u;
     // the runs of planes (quads_eligible checked that each is equally spaced)
     const float* sg[13] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,
                            src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv};
@@ -365,8 +497,10 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
         !encode_plane_group(&maps.state, sg[0], 13, ss, g.R, g.C, g.slots, g.pstride, kSR, kSR) ||
         !encode_plane_group(&maps.consts, cg[0], 19, cs, g.R, g.C, g.slots, g.pstride, kSR, kSR))
         return cudaErrorInvalidValue;
-    const unsigned grid = ctas < a.total ? ctas : a.total;
-    k_iterate_stream<<<grid, kSThreads, stream_smem_bytes(), st>>>(a, maps);
+    if (strips)
+        k_iterate_stream<true><<<grid, kSThreads, stream_smem_bytes(), st>>>(a, maps);
+    else
+        k_iterate_stream<false><<<grid, kSThreads, stream_smem_bytes(), st>>>(a, maps);
     return cudaGetLastError();
 }
 

@@ -212,7 +212,7 @@ static bool level_runs_tiles(const pdflow_solver* s, const LevelGeom& g, unsigne
 }
 
 // Whether level `level`'s tiles run register-resident (quad tiles, form 7, or
-// streamed tiles, forms 8 and 9): chosen for the level and possible at its size
+// streamed tiles and strips, forms 8-10): chosen for the level and possible at its size
 // (rows % 4 == 0; other levels of such a solve run the paired 24x24 tiles,
 // form 5).
 static bool level_runs_quads(const pdflow_solver* s, const LevelGeom& g, unsigned iters, unsigned pairs,
@@ -221,7 +221,7 @@ static bool level_runs_quads(const pdflow_solver* s, const LevelGeom& g, unsigne
     if (!level_runs_tiles(s, g, iters, pairs, level)) return false;
     const int forced = level < 8 ? s->level_form[level] : -1;
     const int form = forced >= 0 ? forced : s->iter_form;
-    return (form >= 7 && form <= 9) && quads_eligible(g, s->L, s->S, s->S);
+    return (form >= 7 && form <= 10) && quads_eligible(g, s->L, s->S, s->S);
 }
 
 // The step-size planes the level's set-up writes for its iteration form.
@@ -250,7 +250,7 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
                                         : (s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok);
     const bool quads = tiles && level_runs_quads(s, g, iters, pairs, level);
     const bool paired = tiles && form >= 3;
-    const int shape = form >= 7 ? 2 : form - 3;   // 40x40, 40x34, 24x24 or 24x28 tiles (forms 7-9 elsewhere: 24x24)
+    const int shape = form >= 7 ? 2 : form - 3;   // 40x40, 40x34, 24x24 or 24x28 tiles (forms 7-10 elsewhere: 24x24)
     if (tiles) {
         State cur = s->S;
         State nxt{s->alt_d[0], s->alt_d[1], s->alt_d[2], s->alt[0], s->alt[1], s->alt[2], s->alt[3], s->alt[4],
@@ -265,7 +265,7 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
             const unsigned kk = (iters - done < h) ? iters - done : h;
             if (quads && form >= 8)
                 CUDA_TRY(launch_iterate_stream(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, s->status,
-                                               unsigned(s->num_sms), halo),
+                                               unsigned(s->num_sms), stream_layout(form)),
                          "streamed tile iteration launch");
             else if (quads)
                 CUDA_TRY(launch_iterate_quads(g, s->L, cur, nxt, p, o.dep, kk, done + kk == iters, st, s->status),

@@ -16,7 +16,8 @@ namespace {
 constexpr TuneCandidate kCandidates[PDFLOW_TUNE_CANDIDATES] = {{0, 0}, {1, 0}, {2, 2}, {2, 3}, {2, 4}, {3, 2}, {3, 3},
                                                             {3, 4}, {4, 2}, {4, 3}, {4, 4}, {5, 2}, {5, 3}, {5, 4},
                                                             {6, 2}, {6, 3}, {6, 4}, {7, 2}, {7, 3}, {7, 4},
-                                                            {8, 2}, {8, 3}, {8, 4}, {9, 4}, {9, 6}, {9, 8}};
+                                                            {8, 2}, {8, 3}, {8, 4}, {9, 4}, {9, 6}, {9, 8},
+                                                               {10, 2}, {10, 3}, {10, 4}};
 
 }  // namespace
 
@@ -38,8 +39,8 @@ extern "C" {
 
 int pdflow_set_level_form(pdflow_solver* s, unsigned level, int form, unsigned iters_per_launch)
 {
-    if (!s || level >= 8 || form < -1 || form > 9 || iters_per_launch > (form == 9 ? 8u : 4u)) {
-        set_last_error("bad argument (form -1..9, level < 8, iterations per launch 0..4, 0..8 for form 9)");
+    if (!s || level >= 8 || form < -1 || form > 10 || iters_per_launch > (form == 9 ? 8u : 4u)) {
+        set_last_error("bad argument (form -1..10, level < 8, iterations per launch 0..4, 0..8 for form 9)");
         return PDFLOW_ERR_ARG;
     }
     drop_graphs(s);

@@ -32,7 +32,8 @@ class Params(ctypes.Structure):
                 ("fovh", ctypes.c_float), ("fovv", ctypes.c_float), ("num_max_iter", ctypes.c_uint * 6)]
 
 
-TUNE_CANDIDATES = 26   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..8 x {2, 3, 4}, form 9 x {4, 6, 8}
+TUNE_CANDIDATES = 29   # PDFLOW_TUNE_CANDIDATES: form 0, form 1, forms 2..8 x {2, 3, 4}, form 9 x {4, 6, 8},
+#                        form 10 x {2, 3, 4}
 
 
 class TuneLevel(ctypes.Structure):

@@ -59,7 +59,7 @@ def test_partial_batch_and_golden(golden_qvga):
 def test_batch_iteration_forms_agree(vga, rows):
     pairs = [scenes.make_pair(200 + k, vga=vga) for k in range(3)]
     a = batch_solve(rows, pairs, form=2)
-    for form in (3, 4, 5, 6, 7, 8, 9, 1, 0):
+    for form in (3, 4, 5, 6, 7, 8, 9, 10, 1, 0):
         b = batch_solve(rows, pairs, form=form)
         for x, y in zip(a, b):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), form

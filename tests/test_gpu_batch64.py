@@ -19,7 +19,7 @@ def test_64_vga_pairs_autotuned_equal_single_solves(built_lib):
     b.push_raw_device(n, i1.data_ptr(), z1.data_ptr())
     b.push_raw_device(n, i2.data_ptr(), z2.data_ptr())
     tune = b.autotune(n)
-    assert [t["form"] for t in tune][-1] in (3, 4, 5, 6, 7, 8)
+    assert [t["form"] for t in tune][-1] in range(3, 11)
     b.solve(n)
     got = b.read_flow(n)
     b.close()

@@ -21,7 +21,7 @@ def _lib(built_lib):
     return built_lib
 
 
-@pytest.mark.parametrize("form", [5, 7, 8, 9])
+@pytest.mark.parametrize("form", [5, 7, 8, 9, 10])
 def test_level_record_equals_the_reference_levels(golden_qvga, form):
     g = golden_qvga
     s = Solver(60, 320, 240, iteration_form=form).initializeCUDA()

@@ -48,7 +48,7 @@ CASES = [("qvga_s0.npz", 240, 320, 240), ("qvga_s0.npz", 60, 320, 240),
          ("vga_s2.npz", 480, 640, 480), ("vga_s2.npz", 240, 640, 480)]
 
 
-@pytest.mark.parametrize("form", [1, 7, 8, 9])
+@pytest.mark.parametrize("form", [1, 7, 8, 9, 10])
 @pytest.mark.parametrize("fixture,rows,w,h", CASES)
 def test_flow_matches_reference_cuda_path(fixture, rows, w, h, form):
     """The final flow equals the reference's own CUDA build bit for bit, with
@@ -202,7 +202,7 @@ def test_iteration_forms_agree(fixture, rows, w, h):
     from conftest import load_golden
     g = load_golden(fixture)
     a = solve(g, rows, w, h, form=2)
-    for form in (1, 0, 5, 7, 8, 9):
+    for form in (1, 0, 5, 7, 8, 9, 10):
         b = solve(g, rows, w, h, form=form)
         for x, y in zip(a, b):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), form
