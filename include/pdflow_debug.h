@@ -24,12 +24,14 @@ typedef void (*pdflow_dump_fn)(void* ctx, const char* name, int level, const flo
  * in CSF_cuda, pdflow_cudalib.h:71-122).  The final flow equals pdflow_solve's. */
 int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
 
-/* Selects how pdflow_solve runs a level's iterations: 10 = as 8 below, but
- * each CTA walks an equal share of the rows of regions left to right and
- * hands each region's last exact column's exchange values to the next one,
- * so that only a right halo is recomputed (28 of 32 columns exact at 4
- * iterations per launch); 9 = as 8 with 16x16 interiors and a halo of 8 (up
- * to 8 iterations per launch); 8 (default) = every
+/* Selects how pdflow_solve runs a level's iterations: 10 (default) = as 8
+ * below, but each CTA walks rows of regions (24-row bands of a pair, or
+ * column pieces of them; taken from a device counter as CTAs finish) left to
+ * right and hands each region's last exact column's exchange values to the
+ * next one, so that only a right halo is recomputed (28 of 32 columns exact
+ * at 4 iterations per launch); levels with fewer bands than SMs run 8
+ * instead; 9 = as 8 with 16x16 interiors and a halo of 8 (up to 8 iterations
+ * per launch); 8 = every
  * level of a batch (more than one pair), and a single pair's levels above 300
  * pixels, as temporally blocked 24x24 tiles (halo 4, up to 4 iterations per
  * launch) walked by one persistent CTA per SM, each tile's state and

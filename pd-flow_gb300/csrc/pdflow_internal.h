@@ -42,7 +42,9 @@ struct pdflow_solver {
     unsigned* flags = nullptr;           // per-CTA progress counters of the grid-form iteration
     unsigned* status = nullptr;          // device status word (0 = ok)
     int num_sms = 0;
-    int iter_form = 8;                   // 8 = streamed register tiles (persistent, one CTA per SM), 7 = quad
+    int iter_form = 10;                  // 10 = streamed strips (levels with a strip per SM; others form 8),
+                                         // 9 = deep streamed tiles,
+                                         // 8 = streamed register tiles (persistent, one CTA per SM), 7 = quad
                                          // register tiles, 5 / 4 / 3 = paired tiles 24x24 (two CTAs per SM) / 40x34 / 40x40,
                                          // 2 = scalar tiles for large levels,
                                          // 1 = one launch per level, 0 = two kernels per iteration

@@ -68,7 +68,9 @@ cudaError_t prepare_quads();
 // of 8 (form 9, up to 8 iterations per launch), or rows of regions walked
 // left to right that carry their left neighbour's exchange values (form 10,
 // 24-row interiors, 32 - kk exact columns per region); same preconditions
-// (quads_eligible) and same bits.
+// (quads_eligible) and same bits.  `status` is the handle's four device
+// words: [0] the status word, [2] and [3] the strip walk's unit counters
+// (zero between launches; the kernel leaves them so).
 enum class StreamLayout { Tiles24, Tiles16, Strips };
 inline StreamLayout stream_layout(int form)
 {

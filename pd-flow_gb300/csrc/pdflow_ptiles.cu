@@ -32,11 +32,15 @@
 // carry of 3 x 32 floats per iteration, in shared memory) instead of
 // recomputing a left halo: after kk iterations columns [x, x + 32 - kk) of a
 // region at column x are exact, 28 of 32 at kk = 4 instead of 24.  The
-// strips (a pair's 24-row bands) are dealt round-robin, so that the CTAs walk
-// vertically adjacent bands side by side (their row halos meet in L2 and
-// their reads fill DRAM pages, as the tiles' do); the strips of a last,
-// partial round are cut into column pieces, one per idle CTA, each starting
-// with a region that recomputes a left halo of kk columns.
+// units of work are whole strips (a pair's 24-row bands) and, for the last
+// strips of the launch, column pieces of them, smaller towards the end (each
+// starting with a region that recomputes a left halo of kk columns).  CTAs take units in order from
+// a device counter as they finish the previous one: they walk vertically
+// adjacent bands side by side (their row halos meet in L2 and their reads
+// fill DRAM pages, as the tiles' do), and a CTA whose strips converge faster
+// (the disc projection's work depends on the data) takes more of them; the
+// pieces keep the last units short.  The last CTA to finish resets the
+// counter for the next launch.
 #include <cuda.h>
 
 #include <algorithm>
@@ -69,8 +73,9 @@ enum { S_DU, S_DV, S_DW, S_UA, S_VA, S_WA, S_PD, S_PUU, S_PUV, S_PVU, S_PVV, S_P
 
 struct StreamArgs {
     LevelGeom g;
-    unsigned strips;           // strips: pairs x tiles_v
-    unsigned pieces;           // strips: pieces per strip of the last, partial round
+    unsigned whole;            // strips: units 0 .. whole-1 are strips 0 .. whole-1
+    unsigned tier_n[3], tier_p[3];   // strips: then tier i: tier_p[i] pieces of each of the next tier_n[i] strips
+    unsigned* work;            // strips: [next unit - grid, CTAs finished], zero between launches
     float* dst[13];            // du dv dw du_acc dv_acc dw_acc pd puu puv pvu pvv pwu pwv (interior written)
     const float* depth_old;
     Params p;
@@ -137,8 +142,8 @@ struct Tile {
     int rv0, ru0, iv0, iv1, iu0, iu1;
     bool more;                   // a region to process
     bool carry_in, carry_out;    // strips: reads / writes the column carry
-    unsigned k;                  // strips: the CTA's segment; tiles: the tile index
-    int c1;                      // strips: the segment's end column
+    unsigned k;                  // strips: the unit; tiles: the tile index
+    int c1;                      // strips: the unit's end column
 };
 
 // Tiles: the launch's tile n (regions of every pair, dealt round-robin).
@@ -162,10 +167,10 @@ __device__ __forceinline__ Tile tile_at(const StreamArgs& a, unsigned n)
     return t;
 }
 
-// Strips: segment k of this CTA's walk, columns [c0, c1) of strip `strip`
-// (strip s is row band s % tiles_v of pair s / tiles_v).  Full rounds: strip
-// k * G + b, all columns; the last round's r strips: piece b / r of strip
-// F * G + b % r.
+// Strips: unit k, columns [c0, c1) of strip `strip` (strip s is row band
+// s % tiles_v of pair s / tiles_v): a whole strip, or piece i of a strip of
+// one of the tiers that follow (within a tier, pieces in order of i, then of
+// the strip).
 struct Segment {
     bool ok;
     unsigned strip;
@@ -173,17 +178,23 @@ struct Segment {
 };
 __device__ __forceinline__ Segment segment(const StreamArgs& a, unsigned k)
 {
-    const unsigned G = gridDim.x, b = blockIdx.x, F = a.strips / G, r = a.strips - F * G;
     const int C = (int)a.g.C;
-    if (k < F) return {true, k * G + b, 0, C};
-    if (k == F && b < r * a.pieces) {
-        const int i = (int)(b / r), n = (int)a.pieces;
-        return {true, F * G + b % r, C * i / n, C * (i + 1) / n};
+    if (k < a.whole) return {true, k, 0, C};
+    unsigned x = k - a.whole, base = a.whole;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const unsigned n = a.tier_n[i], m = a.tier_p[i];
+        if (x < n * m) {
+            const int piece = (int)(x / n);
+            return {true, base + x % n, C * piece / (int)m, C * (piece + 1) / (int)m};
+        }
+        x -= n * m;
+        base += n;
     }
     return {false, 0, 0, 0};
 }
 
-// Strips: the region of segment k whose stored columns start at `col`.  With
+// Strips: the region of unit k whose stored columns start at `col`.  With
 // the carry the region starts at that column; without it, kk columns further
 // left (their values go stale from the left, one column per iteration) or at
 // the image's first column.  Columns up to 32 - kk past the origin are exact
@@ -207,15 +218,17 @@ __device__ __forceinline__ Tile strip_at(const StreamArgs& a, unsigned k, int co
     t.iu0 = col;
     t.iu1 = min(exact, sg.c1);
     t.carry_in = carry;
-    t.carry_out = t.iu1 == exact && t.iu1 < sg.c1;   // the next region continues the segment
+    t.carry_out = t.iu1 == exact && t.iu1 < sg.c1;   // the next region continues the unit
     return t;
 }
 
+// The region after t: the rest of t's unit, else unit `unit` (strips); the
+// CTA's next tile (tiles).
 template <bool kStrips>
-__device__ __forceinline__ Tile next_tile(const StreamArgs& a, const Tile& t)
+__device__ __forceinline__ Tile next_tile(const StreamArgs& a, const Tile& t, unsigned unit)
 {
     if constexpr (kStrips)
-        return t.iu1 < t.c1 ? strip_at(a, t.k, t.iu1, true) : strip_at(a, t.k + 1, -1, false);
+        return t.iu1 < t.c1 ? strip_at(a, t.k, t.iu1, true) : strip_at(a, unit, -1, false);
     else
         return tile_at(a, t.k + gridDim.x);
 }
@@ -251,6 +264,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
 {
     extern __shared__ __align__(128) float sm[];
     __shared__ __align__(8) unsigned long long bar_mem;
+    __shared__ unsigned next_unit;   // strips: the unit thread 0 took for after the current one
     const int t = threadIdx.x;
     const int c = t >> 4, p = t & 15;              // region column, pixel pair
     const int me = c * kSR + 2 * p;                 // the pair's offset in a shared plane
@@ -271,10 +285,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
 
     float* carry = sm + N_PLANES * kSPlane;
     const int cc = kSR - 1 - (int)a.kk;              // strips: the column the next region needs
-    // this CTA's walk: tiles blockIdx.x, + gridDim.x, ...; or its strip segments
+    // this CTA's walk: tiles blockIdx.x, + gridDim.x, ...; or (strips) unit
+    // blockIdx.x, then the units it takes from the counter
     Tile tl;
     if constexpr (kStrips)
-        tl = strip_at(a, 0, -1, false);
+        tl = strip_at(a, blockIdx.x, -1, false);
     else
         tl = tile_at(a, blockIdx.x);
     if (t == 0) {
@@ -307,11 +322,18 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                 if (a.status) atomicExch(a.status, kStreamTimeout);
                 mbar_wait(bar, phase, kStreamWaitLimit);   // bounded: the copies still in flight
             }
-            return;
+            break;
         }
         phase ^= 1u;
         if (t == 0) {
-            const Tile nx = next_tile<kStrips>(a, tl);
+            // the unit after this one (read by every thread after this tile's
+            // iteration barriers; rewritten only after the next tile's first)
+            unsigned unit = 0;
+            if (kStrips && tl.iu1 >= tl.c1) {
+                unit = gridDim.x + atomicAdd(a.work, 1u);
+                next_unit = unit;
+            }
+            const Tile nx = next_tile<kStrips>(a, tl, unit);
             if (nx.more) issue_region(a, tm, sm, bar, nx);
         }
         // the left neighbour's exchange values: the carry of the previous
@@ -435,7 +457,13 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
         }
         // the next tile's staging wait is followed by a barrier before its first
         // exchange store, so the exchange planes (and the carry) need none here
-        tl = next_tile<kStrips>(a, tl);
+        tl = next_tile<kStrips>(a, tl, kStrips ? next_unit : 0u);
+    }
+    // strips: the last CTA to finish (every CTA has taken its last unit)
+    // clears the counter for the next launch
+    if (kStrips && t == 0 && atomicAdd(a.work + 1, 1u) == gridDim.x - 1) {
+        atomicExch(a.work, 0u);
+        atomicExch(a.work + 1, 0u);
     }
 }
 
@@ -480,12 +508,26 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     a.tiles_v = (g.R + kST - 1) / kST;
     a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
     a.total = a.tiles * g.pairs;
-    a.strips = g.pairs * a.tiles_v;
     const unsigned grid = ctas < a.total ? ctas : a.total;
-    // pieces of the last round's strips: one per idle CTA, at least 32 - 2 kk
-    // exact columns each
-    const unsigned rest = a.strips % grid, most = (g.C + (kSR - 2 * kk) - 1) / (kSR - 2 * kk);
-    a.pieces = rest ? std::max(1u, std::min(grid / rest, most)) : 1u;
+    // strip units: the last grid / 4 strips in 8 pieces, the grid / 2 before
+    // them in 4, the grid before those in 2, the rest whole; no more strips
+    // than CTAs: every strip in as many pieces as CTAs allow.  Pieces are at
+    // least one restart region's 32 - 2 kk exact columns wide.
+    const unsigned strips_n = g.pairs * a.tiles_v, most = (g.C + (kSR - 2 * kk) - 1) / (kSR - 2 * kk);
+    unsigned left = strips_n;
+    const unsigned tn[3] = {grid, grid / 2, grid / 4}, tp[3] = {2, 4, 8};
+    for (int i = 2; i >= 0; --i) {
+        a.tier_n[i] = strips_n > grid ? std::min(tn[i], left) : 0u;
+        a.tier_p[i] = std::min(tp[i], most);
+        left -= a.tier_n[i];
+    }
+    if (strips_n <= grid) {
+        a.tier_n[0] = strips_n;
+        a.tier_p[0] = std::max(1u, std::min(grid / strips_n, most));
+        left = 0;
+    }
+    a.whole = left;
+    a.work = status + 2;
     // the runs of planes (quads_eligible checked that each is equally spaced)
     const float* sg[13] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,
                            src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv};

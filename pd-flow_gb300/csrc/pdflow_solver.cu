@@ -90,7 +90,7 @@ int check_status(pdflow_solver* s)
     CUDA_TRY(cudaMemcpyAsync(&st, s->status, sizeof st, cudaMemcpyDeviceToHost, s->stream), "status read");
     CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
     if (st != 0) {
-        CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof st, s->stream), "status reset");
+        CUDA_TRY(cudaMemsetAsync(s->status, 0, 4 * sizeof st, s->stream), "status reset");   // and the strip counters
         CUDA_TRY(cudaStreamSynchronize(s->stream), "synchronize");
         return set_error(PDFLOW_ERR_TIMEOUT, "a bounded device-side wait gave up (iteration neighbour sync)");
     }
@@ -211,6 +211,18 @@ static bool level_runs_tiles(const pdflow_solver* s, const LevelGeom& g, unsigne
     return s->iter_form >= 2 && iters > 0 && (pairs > 1 || g.N > 300u);
 }
 
+// The level's iteration form: its autotuned or hand-set form, else the
+// handle's.  By default the strips (form 10) run only where the level has a
+// strip (a pair's 24-row band) for every SM; smaller levels run the streamed
+// tiles (form 8), which deal fewer pixels to every SM.
+static int level_form(const pdflow_solver* s, const LevelGeom& g, unsigned pairs, unsigned level)
+{
+    const int forced = level < 8 ? s->level_form[level] : -1;
+    if (forced >= 0) return forced;
+    if (s->iter_form == 10 && pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms)) return 8;
+    return s->iter_form;
+}
+
 // Whether level `level`'s tiles run register-resident (quad tiles, form 7, or
 // streamed tiles and strips, forms 8-10): chosen for the level and possible at its size
 // (rows % 4 == 0; other levels of such a solve run the paired 24x24 tiles,
@@ -219,8 +231,7 @@ static bool level_runs_quads(const pdflow_solver* s, const LevelGeom& g, unsigne
                              unsigned level)
 {
     if (!level_runs_tiles(s, g, iters, pairs, level)) return false;
-    const int forced = level < 8 ? s->level_form[level] : -1;
-    const int form = forced >= 0 ? forced : s->iter_form;
+    const int form = level_form(s, g, pairs, level);
     return (form >= 7 && form <= 10) && quads_eligible(g, s->L, s->S, s->S);
 }
 
@@ -245,7 +256,7 @@ static int enqueue_iterations(pdflow_solver* s, cudaStream_t st, const LevelGeom
     const int forced = level < 8 ? s->level_form[level] : -1;
     const bool one_launch_ok = (pairs == 1 || pl.mode != kIterGrid) && pl.smem_bytes <= iterate_smem_limit();
     const bool tiles = level_runs_tiles(s, g, iters, pairs, level);
-    const int form = forced >= 0 ? forced : s->iter_form;
+    const int form = level_form(s, g, pairs, level);
     const bool one_launch = forced >= 0 ? (forced == 1 && iters > 0 && one_launch_ok)
                                         : (s->iter_form >= 1 && iters > 0 && !tiles && one_launch_ok);
     const bool quads = tiles && level_runs_quads(s, g, iters, pairs, level);

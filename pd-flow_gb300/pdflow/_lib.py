@@ -363,7 +363,7 @@ class Solver(_Extras):
     freeGPUMemory."""
 
     def __init__(self, rows: int = 240, width: int = 320, height: int = 240, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 8):
+                 use_graph: bool = True, iteration_form: int = 10):
         self.rows, self.width, self.height = rows, width, height
         self.cols = rows * 320 // 240
         self.params = params
@@ -508,7 +508,7 @@ class BatchSolver(_Extras):
     a camera stream that keeps its previous frame on the device."""
 
     def __init__(self, rows: int, width: int, height: int, max_pairs: int, params: Params | None = None,
-                 use_graph: bool = True, iteration_form: int = 8):
+                 use_graph: bool = True, iteration_form: int = 10):
         lib = load()
         self.rows, self.width, self.height, self.max_pairs = rows, width, height, max_pairs
         self.cols = rows * 320 // 240

@@ -19,7 +19,7 @@ def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--rows", type=int, default=480, choices=(60, 120, 240, 480))
     ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--form", type=int, default=8, choices=tuple(range(11)))
+    ap.add_argument("--form", type=int, default=10, choices=tuple(range(11)))
     ap.add_argument("--learned", type=float, default=0.0,
                     help="iteration scale of a learned warm-started solve (0: plain solve)")
     ap.add_argument("--solves", type=int, default=2)
