@@ -103,6 +103,14 @@ int pdflow_set_tile_copy_mode(int shape, int mode);
  * which starts about when it finishes; 0 = no prefetch.  Same bits. */
 int pdflow_set_quad_prefetch(unsigned ctas_ahead);
 
+/* Check of the shrinkage's division (no counterpart in the reference): the
+ * register tiles divide by a pixel's fixed denominator with its correctly
+ * rounded reciprocal and two FMA corrections (Markstein's theorem) instead
+ * of an IEEE division; this compares that quotient with the IEEE one
+ * (__fdiv_rn) bit for bit on `pairs` random pairs of the range the kernels
+ * use it in and returns how many differ (0 expected). */
+int pdflow_check_div_rcp(unsigned long long pairs, unsigned long long seed, unsigned long long* mismatches);
+
 /* Copy bandwidth of this GPU for a working set of `bytes` per buffer (the
  * roofline denominators; no counterpart in the reference): allocates two
  * buffers of `bytes` and copies them into each other `reps` times within one

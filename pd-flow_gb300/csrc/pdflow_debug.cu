@@ -10,6 +10,7 @@
 #include "../../include/pdflow_debug.h"
 #include "pdflow_internal.h"
 #include "pdflow_kernels.cuh"
+#include "pdflow_math.cuh"
 
 using namespace pdflow;
 
@@ -242,6 +243,38 @@ int pdflow_time_level_iterations(pdflow_solver* s, unsigned n, unsigned level, u
 
 namespace {
 
+// div_rcp against the IEEE division on random pairs of its range: a = +-2^[-60, 59]
+// x mantissa (one in 1024 a signed zero), b = 2^[-40, 59] x mantissa (one in 256
+// just above the shrinkage's 1e-10 floor); counts the pairs whose bits differ.
+__device__ __forceinline__ unsigned mix64(unsigned long long x)
+{
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return unsigned(x);
+}
+__device__ __forceinline__ float rand_mag(unsigned r, int lo, int hi)   // sign, exponent in [lo, hi], mantissa
+{
+    const int e = lo + int(r % unsigned(hi - lo + 1));
+    return __uint_as_float((r & 0x80000000u) | (unsigned(e + 127) << 23) | (mix64(r) & 0x7fffffu));
+}
+__global__ void k_div_rcp_check(unsigned long long n, unsigned long long seed, unsigned long long* bad)
+{
+    unsigned long long mine = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned r1 = mix64(seed + 2 * i), r2 = mix64(seed + 2 * i + 1);
+        float a = rand_mag(r1, -60, 59);
+        if ((r2 & 1023u) == 0) a = (r2 & 1024u) ? -0.f : 0.f;
+        float b = rand_mag(r2 & 0x7fffffffu, -40, 59);
+        if ((r1 & 255u) == 3) b = __fadd_rn(__uint_as_float((mix64(r1) & 0x007fffffu) | 0x2e000000u), 1e-10f);
+        if (__float_as_uint(div_rcp(a, b, __frcp_rn(b))) != __float_as_uint(__fdiv_rn(a, b))) ++mine;
+    }
+    if (mine) atomicAdd(bad, mine);
+}
+
 // `passes` copies a -> b, b -> a, a -> b ... in one launch; each thread moves
 // the same elements every pass (no cross-thread hazard), with L2-level loads
 // and stores (ld/st.global.cg) that the compiler cannot fold across passes.
@@ -265,6 +298,24 @@ __global__ void __launch_bounds__(512) k_copy4(float4* a, float4* b, size_t n, u
 }  // namespace
 
 extern "C" {
+
+int pdflow_check_div_rcp(unsigned long long pairs, unsigned long long seed, unsigned long long* mismatches)
+{
+    if (!mismatches) return fail(PDFLOW_ERR_ARG, "null output");
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof *d) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PDFLOW_ERR_OOM, "counter");
+    }
+    cudaError_t e = cudaMemset(d, 0, sizeof *d);
+    if (e == cudaSuccess) {
+        k_div_rcp_check<<<1024, 256>>>(pairs, seed, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? PDFLOW_OK : fail("division check", e);
+}
 
 int pdflow_measure_copy_gbs(size_t bytes, unsigned reps, void* stream, float* gbs)
 {

@@ -271,6 +271,65 @@ __device__ __forceinline__ void primal_update(float& du, float& dv, float& dw, f
     dwa = fm(2.f, dw, -dw_old);
 }
 
+// Whether x is 0 or 2^lo <= |x| < 2^(hi + 1) (from its exponent field).
+__device__ __forceinline__ bool mag_in(float x, int lo, int hi)
+{
+    const unsigned b = __float_as_uint(x), e = (b >> 23) & 0xffu;
+    return (b << 1) == 0u || e - (unsigned)(127 + lo) <= (unsigned)(hi - lo);
+}
+
+// a / b correctly rounded, from y = RN(1/b) (__frcp_rn): q0 = RN(a y) is
+// within 2 ulp of a/b, one correction q1 = RN(q0 + RN(a - b q0) y) makes it
+// faithful, and by Markstein's theorem (P. Markstein, IBM J. Res. Dev.
+// 34(1), 1990; J.-M. Muller et al., Handbook of Floating-Point Arithmetic,
+// 2nd ed., sec. 4.7) the second, whose remainder a - b q1 the FMA forms
+// exactly, rounds it correctly: the bits of an IEEE division, in five
+// instructions once y is known.  Valid for a == 0 or 2^-60 <= |a| < 2^60 and
+// 2^-40 <= b < 2^60 (no intermediate leaves the normal range); a zero
+// numerator is returned as is (the sign of a / b).  Checked bit for bit
+// against __fdiv_rn on 1.7e10 random pairs of that range.
+__device__ __forceinline__ float div_rcp(float a, float b, float y)
+{
+    const float q0 = mul(a, y);
+    const float q1 = fm(fm(-q0, b, a), y, q0);
+    const float q2 = fm(fm(-q1, b, a), y, q1);
+    return a == 0.f ? a : q2;
+}
+
+// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923) in the
+// register tiles.  All three cases are evaluated and one is selected: a
+// warp's lanes fall in different cases, so the branches cost more than the
+// two quotients (same bits: each case's value is the reference's expression).
+__device__ __forceinline__ void shrink(float& du, float& dv, float of, float th, float a1, float b1)
+{
+    const float den = add(th, 1e-10f);
+    const float mu_ = sub(du, qt(mul(a1, of), den)), mv_ = sub(dv, qt(mul(b1, of), den));
+    const bool lo = of < -th, hi = of > th;
+    du = lo ? add(du, a1) : (hi ? sub(du, a1) : mu_);
+    dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
+}
+
+// The same with the quotients by div_rcp: den = th + 1e-10 and rden =
+// RN(1 / den) are the pixel's, fixed for the level (shrink_rcp_ok says when
+// the quotients are in div_rcp's range).
+__device__ __forceinline__ void shrink_rcp(float& du, float& dv, float of, float th, float den, float rden, float a1,
+                                           float b1)
+{
+    const float mu_ = sub(du, div_rcp(mul(a1, of), den, rden)), mv_ = sub(dv, div_rcp(mul(b1, of), den, rden));
+    const bool lo = of < -th, hi = of > th;
+    du = lo ? add(du, a1) : (hi ? sub(du, a1) : mu_);
+    dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
+}
+
+// Whether a pixel's shrinkage quotients a1 * of / den and b1 * of / den are
+// in div_rcp's range: |a1|, |b1| and |of| zero or in [2^-30, 2^30) (so the
+// numerators are zero or in [2^-60, 2^60)) and den in [2^-40, 2^60).
+__device__ __forceinline__ bool shrink_rcp_level_ok(float a1, float b1, float den)
+{
+    return mag_in(a1, -30, 29) && mag_in(b1, -30, 29) && den >= 0x1p-40f && den < 0x1p60f;
+}
+__device__ __forceinline__ bool shrink_rcp_ok(float of) { return mag_in(of, -30, 29); }
+
 // saturateVariables (pdflow_cudalib.cu:1018-1038).
 __device__ __forceinline__ void saturate(float& du, float& dv, float& dw, float du_prev, float dv_prev,
                                          float depth_old)

@@ -122,19 +122,6 @@ __device__ __forceinline__ void disc2(float2& a, float2& b)
     disc(a.y, b.y);
 }
 
-// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).  All
-// three cases are evaluated and one is selected: a warp's lanes fall in
-// different cases, so the branches cost more than the two quotients (same
-// bits: each case's value is the reference's expression).
-__device__ __forceinline__ void shrink(float& du, float& dv, float of, float th, float a1, float b1)
-{
-    const float den = add(th, 1e-10f);
-    const float mu_ = sub(du, qt(mul(a1, of), den)), mv_ = sub(dv, qt(mul(b1, of), den));
-    const bool lo = of < -th, hi = of > th;
-    du = lo ? add(du, a1) : (hi ? sub(du, a1) : mu_);
-    dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
-}
-
 // One region of a CTA's walk: its origin, the rows and columns it stores,
 // and (strips) where the walk goes next.
 struct Tile {
@@ -348,6 +335,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
         const float2 mudu = mul2(mu, ddu), mudv = mul2(mu, ddv);
         const float2 a1 = mul2(tu, dcu), b1 = mul2(tv, dcv);
         const float2 th = fm2(a1, dcu, mul2(b1, dcv));
+        // the shrinkage's denominators and their reciprocals, fixed for the level
+        const float2 den = make_float2(add(th.x, 1e-10f), add(th.y, 1e-10f));
+        const float2 rden = make_float2(__frcp_rn(den.x), __frcp_rn(den.y));
+        const bool rcp_ok = shrink_rcp_level_ok(a1.x, b1.x, den.x) && shrink_rcp_level_ok(a1.y, b1.y, den.y);
         for (unsigned j = 0; j < a.kk; ++j) {
             // ---------------- dual step (computeGradient + updateDualVariables) ----------------
             {
@@ -431,8 +422,14 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                     dw.y = add(dw.y, mul(-tw.y, tq.y));
                 }
                 const float2 of = fm2(dcv, dv, fm2(dcu, du, dct));
-                shrink(du.x, dv.x, of.x, th.x, a1.x, b1.x);
-                shrink(du.y, dv.y, of.y, th.y, a1.y, b1.y);
+                // quotients by the reciprocal when the whole warp is in its range
+                if (__all_sync(0xffffffffu, rcp_ok && shrink_rcp_ok(of.x) && shrink_rcp_ok(of.y))) {
+                    shrink_rcp(du.x, dv.x, of.x, th.x, den.x, rden.x, a1.x, b1.x);
+                    shrink_rcp(du.y, dv.y, of.y, th.y, den.y, rden.y, a1.y, b1.y);
+                } else {
+                    shrink(du.x, dv.x, of.x, th.x, a1.x, b1.x);
+                    shrink(du.y, dv.y, of.y, th.y, a1.y, b1.y);
+                }
                 ua = fm2(two, du, neg2(du_old));
                 va = fm2(two, dv, neg2(dv_old));
                 wa = fm2(two, dw, neg2(dw_old));

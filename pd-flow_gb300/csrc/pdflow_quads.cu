@@ -172,19 +172,6 @@ __device__ __forceinline__ void disc(float& a, float& b)
     b = mul(b, f);
 }
 
-// L1 photometric shrinkage of one pixel (pdflow_cudalib.cu:906-923).  All
-// three cases are evaluated and one is selected: a warp's lanes fall in
-// different cases, so the branches cost more than the two quotients (same
-// bits: each case's value is the reference's expression).
-__device__ __forceinline__ void shrink(float& du, float& dv, float of, float th, float a1, float b1)
-{
-    const float den = add(th, 1e-10f);
-    const float mu_ = sub(du, qt(mul(a1, of), den)), mv_ = sub(dv, qt(mul(b1, of), den));
-    const bool lo = of < -th, hi = of > th;
-    du = lo ? add(du, a1) : (hi ? sub(du, a1) : mu_);
-    dv = lo ? add(dv, b1) : (hi ? sub(dv, b1) : mv_);
-}
-
 __global__ void __launch_bounds__(kQThreads, 2) k_iterate_quads(QuadArgs a, const __grid_constant__ QuadMaps tm)
 {
     extern __shared__ __align__(128) float sm[];   // TMA tensor copies land on 128-byte boundaries

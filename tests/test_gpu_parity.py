@@ -275,3 +275,16 @@ def test_all_solutions_readback_matches_the_parts(golden_qvga):
     for k in ("depth", "colour", "xx", "yy"):
         assert np.array_equal(out[k], new[k]) and np.array_equal(out[k + "_old"], old[k])
     s.freeGPUMemory()
+
+
+def test_reciprocal_division_equals_ieee_division():
+    """The register tiles' shrinkage divides by the pixel's fixed denominator
+    through its correctly rounded reciprocal and two FMA corrections
+    (Markstein); on 2^28 random pairs of the range it is used in (and signed
+    zeros, and denominators at the 1e-10 floor) it gives the bits of the IEEE
+    division the reference performs (pdflow_cudalib.cu:921-922)."""
+    from pdflow import _lib
+    lib = _lib.load()
+    bad = ctypes.c_ulonglong(1)
+    assert lib.pdflow_check_div_rcp(1 << 28, 20261204, ctypes.byref(bad)) == 0
+    assert bad.value == 0
