@@ -44,6 +44,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "pdflow_iterate.cuh"
 #include "pdflow_math.cuh"
@@ -339,111 +340,123 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
         const float2 den = make_float2(add(th.x, 1e-10f), add(th.y, 1e-10f));
         const float2 rden = make_float2(__frcp_rn(den.x), __frcp_rn(den.y));
         const bool rcp_ok = shrink_rcp_level_ok(a1.x, b1.x, den.x) && shrink_rcp_level_ok(a1.y, b1.y, den.y);
-        for (unsigned j = 0; j < a.kk; ++j) {
-            // ---------------- dual step (computeGradient + updateDualVariables) ----------------
-            {
-                const float2 U = add2(ua, dup), V = add2(va, dvp);
-                *reinterpret_cast<float2*>(XU + me) = U;
-                *reinterpret_cast<float2*>(XV + me) = V;
-                *reinterpret_cast<float2*>(XW + me) = wa;
-                const float Ub = __shfl_down_sync(0xffffffffu, U.x, 1, 16);   // the next pair's first row
-                const float Vb = __shfl_down_sync(0xffffffffu, V.x, 1, 16);
-                const float Wb = __shfl_down_sync(0xffffffffu, wa.x, 1, 16);
-                __syncthreads();
-                // borders by selects, not branches (the neighbour slot at the
-                // region's right edge is the thread's own: read, then dropped)
-                float2 gu1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XU + right), U));
-                float2 gv1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XV + right), V));
-                float2 gw1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XW + right), wa));
-                if (lu) {
-                    gu1 = zero;
-                    gv1 = zero;
-                    gw1 = zero;
-                }
-                float2 gu2 = mul2(rj, sub2(make_float2(U.y, Ub), U));
-                float2 gv2 = mul2(rj, sub2(make_float2(V.y, Vb), V));
-                float2 gw2 = mul2(rj, sub2(make_float2(wa.y, Wb), wa));
-                if (lv) {
-                    gu2.y = 0.f;
-                    gv2.y = 0.f;
-                    gw2.y = 0.f;
-                }
-                const float2 X = fm2(ddv, va, fm2(ddu, ua, sub2(ddt, wa)));
-                pd = fm2(s0, X, pd);
-                puu = fm2(s1, gu1, puu);
-                puv = fm2(s2, gu2, puv);
-                pvu = fm2(s1, gv1, pvu);
-                pvv = fm2(s2, gv2, pvv);
-                pwu = fm2(s3, gw1, pwu);
-                pwv = fm2(s4, gw2, pwv);
-                pd.x = clamp1(pd.x);
-                pd.y = clamp1(pd.y);
-                disc2(puu, puv);
-                disc2(pvu, pvv);
-                disc2(pwu, pwv);
-            }
-            // ---------------- primal step (computeDivergence + updatePrimalVariables) ----------------
-            {
-                const float2 yu = mul2(ri, puu), yv = mul2(ri, pvu), yw = mul2(ri, pwu);
-                *reinterpret_cast<float2*>(YU + me) = yu;
-                *reinterpret_cast<float2*>(YV + me) = yv;
-                *reinterpret_cast<float2*>(YW + me) = yw;
-                if (to_carry) {
-                    float* y = yc + j * (3 * kSR);
-                    *reinterpret_cast<float2*>(y) = yu;
-                    *reinterpret_cast<float2*>(y + kSR) = yv;
-                    *reinterpret_cast<float2*>(y + 2 * kSR) = yw;
-                }
-                const float2 zu = mul2(rj, puv), zv = mul2(rj, pvv), zw = mul2(rj, pwv);
-                const float zua = __shfl_up_sync(0xffffffffu, zu.y, 1, 16);   // the previous pair's second row
-                const float zva = __shfl_up_sync(0xffffffffu, zv.y, 1, 16);
-                const float zwa = __shfl_up_sync(0xffffffffu, zw.y, 1, 16);
-                __syncthreads();
-                const float2 pu_[3] = {puu, pvu, pwu}, pv_[3] = {puv, pvv, pwv};
-                const float2 zm_[3] = {make_float2(zua, zu.x), make_float2(zva, zv.x), make_float2(zwa, zw.x)};
-                float2 div[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const float2 ym = neg2(*reinterpret_cast<const float2*>(yl + k * yl_k + (int)j * yl_j));
-                    const float2 dm = fm2(ri, pu_[k], ym), df = mul2(ri, pu_[k]);
-                    float2 d = fu ? df : (lu ? ym : dm);   // first / last / inner column
-                    float2 g = add2(d, fm2(rj, pv_[k], neg2(zm_[k])));
-                    if (fv) g.x = fm(rj.x, pv_[k].x, d.x);
-                    if (lv) g.y = fm(-rj.x, pv_[k].x, d.y);
-                    div[k] = g;
-                }
-                const float2 du_old = du, dv_old = dv, dw_old = dw;
-                du = fm2(neg2(tu), fm2(mudu, pd, neg2(mul2(li2, div[0]))), du);
-                dv = fm2(neg2(tv), fm2(mudv, pd, neg2(mul2(li2, div[1]))), dv);
+        // the iterations, with the image-border cases (kBorder) or, for a region
+        // that touches no image border, without them (the same expressions)
+        auto iterate = [&](auto border) {
+            constexpr bool kBorder = decltype(border)::value;
+            for (unsigned j = 0; j < a.kk; ++j) {
+                // ---------------- dual step (computeGradient + updateDualVariables) ----------------
                 {
-                    // per lane: see pdflow_pack.cuh on contraction of packed products
-                    const float2 tq = fm2(neg2(mu), pd, neg2(mul2(ld2, div[2])));
-                    dw.x = add(dw.x, mul(-tw.x, tq.x));
-                    dw.y = add(dw.y, mul(-tw.y, tq.y));
+                    const float2 U = add2(ua, dup), V = add2(va, dvp);
+                    *reinterpret_cast<float2*>(XU + me) = U;
+                    *reinterpret_cast<float2*>(XV + me) = V;
+                    *reinterpret_cast<float2*>(XW + me) = wa;
+                    const float Ub = __shfl_down_sync(0xffffffffu, U.x, 1, 16);   // the next pair's first row
+                    const float Vb = __shfl_down_sync(0xffffffffu, V.x, 1, 16);
+                    const float Wb = __shfl_down_sync(0xffffffffu, wa.x, 1, 16);
+                    __syncthreads();
+                    // borders by selects, not branches (the neighbour slot at the
+                    // region's right edge is the thread's own: read, then dropped)
+                    float2 gu1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XU + right), U));
+                    float2 gv1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XV + right), V));
+                    float2 gw1 = mul2(ri, sub2(*reinterpret_cast<const float2*>(XW + right), wa));
+                    if (kBorder && lu) {
+                        gu1 = zero;
+                        gv1 = zero;
+                        gw1 = zero;
+                    }
+                    float2 gu2 = mul2(rj, sub2(make_float2(U.y, Ub), U));
+                    float2 gv2 = mul2(rj, sub2(make_float2(V.y, Vb), V));
+                    float2 gw2 = mul2(rj, sub2(make_float2(wa.y, Wb), wa));
+                    if (kBorder && lv) {
+                        gu2.y = 0.f;
+                        gv2.y = 0.f;
+                        gw2.y = 0.f;
+                    }
+                    const float2 X = fm2(ddv, va, fm2(ddu, ua, sub2(ddt, wa)));
+                    pd = fm2(s0, X, pd);
+                    puu = fm2(s1, gu1, puu);
+                    puv = fm2(s2, gu2, puv);
+                    pvu = fm2(s1, gv1, pvu);
+                    pvv = fm2(s2, gv2, pvv);
+                    pwu = fm2(s3, gw1, pwu);
+                    pwv = fm2(s4, gw2, pwv);
+                    pd.x = clamp1(pd.x);
+                    pd.y = clamp1(pd.y);
+                    disc2(puu, puv);
+                    disc2(pvu, pvv);
+                    disc2(pwu, pwv);
                 }
-                const float2 of = fm2(dcv, dv, fm2(dcu, du, dct));
-                // quotients by the reciprocal when the whole warp is in its range
-                if (__all_sync(0xffffffffu, rcp_ok && shrink_rcp_ok(of.x) && shrink_rcp_ok(of.y))) {
-                    shrink_rcp(du.x, dv.x, of.x, th.x, den.x, rden.x, a1.x, b1.x);
-                    shrink_rcp(du.y, dv.y, of.y, th.y, den.y, rden.y, a1.y, b1.y);
-                } else {
-                    shrink(du.x, dv.x, of.x, th.x, a1.x, b1.x);
-                    shrink(du.y, dv.y, of.y, th.y, a1.y, b1.y);
+                // ---------------- primal step (computeDivergence + updatePrimalVariables) ----------------
+                {
+                    const float2 yu = mul2(ri, puu), yv = mul2(ri, pvu), yw = mul2(ri, pwu);
+                    *reinterpret_cast<float2*>(YU + me) = yu;
+                    *reinterpret_cast<float2*>(YV + me) = yv;
+                    *reinterpret_cast<float2*>(YW + me) = yw;
+                    if (to_carry) {
+                        float* y = yc + j * (3 * kSR);
+                        *reinterpret_cast<float2*>(y) = yu;
+                        *reinterpret_cast<float2*>(y + kSR) = yv;
+                        *reinterpret_cast<float2*>(y + 2 * kSR) = yw;
+                    }
+                    const float2 zu = mul2(rj, puv), zv = mul2(rj, pvv), zw = mul2(rj, pwv);
+                    const float zua = __shfl_up_sync(0xffffffffu, zu.y, 1, 16);   // the previous pair's second row
+                    const float zva = __shfl_up_sync(0xffffffffu, zv.y, 1, 16);
+                    const float zwa = __shfl_up_sync(0xffffffffu, zw.y, 1, 16);
+                    __syncthreads();
+                    const float2 pu_[3] = {puu, pvu, pwu}, pv_[3] = {puv, pvv, pwv};
+                    const float2 zm_[3] = {make_float2(zua, zu.x), make_float2(zva, zv.x), make_float2(zwa, zw.x)};
+                    float2 div[3];
+    #pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const float2 ym = neg2(*reinterpret_cast<const float2*>(yl + k * yl_k + (int)j * yl_j));
+                        float2 d = fm2(ri, pu_[k], ym);
+                        // first / last / inner column
+                        if constexpr (kBorder) d = fu ? mul2(ri, pu_[k]) : (lu ? ym : d);
+                        float2 g = add2(d, fm2(rj, pv_[k], neg2(zm_[k])));
+                        if constexpr (kBorder) {
+                            if (fv) g.x = fm(rj.x, pv_[k].x, d.x);
+                            if (lv) g.y = fm(-rj.x, pv_[k].x, d.y);
+                        }
+                        div[k] = g;
+                    }
+                    const float2 du_old = du, dv_old = dv, dw_old = dw;
+                    du = fm2(neg2(tu), fm2(mudu, pd, neg2(mul2(li2, div[0]))), du);
+                    dv = fm2(neg2(tv), fm2(mudv, pd, neg2(mul2(li2, div[1]))), dv);
+                    {
+                        // per lane: see pdflow_pack.cuh on contraction of packed products
+                        const float2 tq = fm2(neg2(mu), pd, neg2(mul2(ld2, div[2])));
+                        dw.x = add(dw.x, mul(-tw.x, tq.x));
+                        dw.y = add(dw.y, mul(-tw.y, tq.y));
+                    }
+                    const float2 of = fm2(dcv, dv, fm2(dcu, du, dct));
+                    // quotients by the reciprocal when the whole warp is in its range
+                    if (__all_sync(0xffffffffu, rcp_ok && shrink_rcp_ok(of.x) && shrink_rcp_ok(of.y))) {
+                        shrink_rcp(du.x, dv.x, of.x, th.x, den.x, rden.x, a1.x, b1.x);
+                        shrink_rcp(du.y, dv.y, of.y, th.y, den.y, rden.y, a1.y, b1.y);
+                    } else {
+                        shrink(du.x, dv.x, of.x, th.x, a1.x, b1.x);
+                        shrink(du.y, dv.y, of.y, th.y, a1.y, b1.y);
+                    }
+                    ua = fm2(two, du, neg2(du_old));
+                    va = fm2(two, dv, neg2(dv_old));
+                    wa = fm2(two, dw, neg2(dw_old));
+                    if (last_launch && j + 1 == a.kk && live) {
+                        // saturateVariables (pdflow_cudalib.cu:1018-1038) after the level's last iteration
+                        const float2 z = __ldg(reinterpret_cast<const float2*>(at(a.depth_old, po) + v0 +
+                                                                                (size_t)u * (size_t)R));
+                        saturate(du.x, dv.x, dw.x, dup.x, dvp.x, z.x);
+                        saturate(du.y, dv.y, dw.y, dup.y, dvp.y, z.y);
+                    }
                 }
-                ua = fm2(two, du, neg2(du_old));
-                va = fm2(two, dv, neg2(dv_old));
-                wa = fm2(two, dw, neg2(dw_old));
-                if (last_launch && j + 1 == a.kk && live) {
-                    // saturateVariables (pdflow_cudalib.cu:1018-1038) after the level's last iteration
-                    const float2 z = __ldg(reinterpret_cast<const float2*>(at(a.depth_old, po) + v0 +
-                                                                            (size_t)u * (size_t)R));
-                    saturate(du.x, dv.x, dw.x, dup.x, dvp.x, z.x);
-                    saturate(du.y, dv.y, dw.y, dup.y, dvp.y, z.y);
-                }
+                // no barrier here: this iteration's exchange reads happen before the next
+                // one's first barrier, and the next stores to the same planes after it
             }
-            // no barrier here: this iteration's exchange reads happen before the next
-            // one's first barrier, and the next stores to the same planes after it
-        }
+        };
+        if (tl.ru0 > 0 && tl.ru0 + kSR < C && tl.rv0 > 0 && tl.rv0 + kSR < R)   // the same for the whole CTA
+            iterate(std::false_type{});
+        else
+            iterate(std::true_type{});
 
         // ---- the interior to the destination buffer ----
         if (live && v0 >= tl.iv0 && v0 < tl.iv1 && u >= tl.iu0 && u < tl.iu1) {
