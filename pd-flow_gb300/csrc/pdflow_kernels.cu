@@ -177,85 +177,70 @@ __global__ void k_pyr_down(PyrLevel prev, unsigned R, unsigned C, PyrLevel out, 
 // Level set-up
 // ---------------------------------------------------------------------------
 
-// assignZeros + upsampleCopy/upsampleFilterPrevSolution (pdflow_cudalib.cu:
-// 439-569) as a gather over the coarse solution (the zero-inserted taps
-// contribute exactly zero and are skipped), followed by computeRij (:725-779).
-__global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S,
-                             const float* __restrict__ seed)
+// upsampleCopy + upsampleFilterPrevSolution (pdflow_cudalib.cu:460-569) at one
+// pixel, as a gather over the coarse solution (the zero-inserted taps
+// contribute exactly zero and are skipped): acc = du dv dw pd puu puv pvu pvv
+// pwu pwv, the taps in the reference's order (row offset, then column).
+__device__ __forceinline__ void upsample_px(const LevelSol& cs, unsigned v, unsigned u, unsigned R, unsigned C,
+                                            float (&acc)[10])
 {
-    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
-    cs = at(cs, po);
-    o = at(o, po);
-    n = at(n, po);
-    L = at(L, po);
-    S = at(S, po);
-    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
-    if (index >= g.N) return;
-    const unsigned R = g.R, C = g.C;
-    const unsigned v = index % R, u = index / R;
-
-    float du = 0.f, dv = 0.f, dw = 0.f, pd = 0.f, puu = 0.f, puv = 0.f, pvu = 0.f, pvv = 0.f, pwu = 0.f, pwv = 0.f;
-    if (seed) {   // warm start: a predicted solution of this level, duals from zero
-        const float* sp = seed + (size_t)blockIdx.y * 3 * g.N;
-        du = sp[index];
-        dv = sp[g.N + index];
-        dw = sp[2 * g.N + index];
-    } else if (!first) {
-        const unsigned Rc = R / 2;
-        const bool inner = (v > 1) && (v < R - 2) && (u > 1) && (u < C - 2);
-        float acu_weight = 1.f;
+    const unsigned Rc = R / 2;
+    const bool inner = (v > 1) && (v < R - 2) && (u > 1) && (u < C - 2);
 #pragma unroll
-        for (int k = -2; k < 3; k++)
+    for (int q = 0; q < 10; ++q) acc[q] = 0.f;
+    float acu_weight = 1.f;
 #pragma unroll
-            for (int l = -2; l < 3; l++) {
-                const int indv = (int)v + k, indu = (int)u + l;
-                const float gm4 = mul(4.f, gmask(k, l));
-                if ((indv < 0) || (indv >= (int)R) || (indu < 0) || (indu >= (int)C)) {
-                    acu_weight = sub(acu_weight, mul(0.25f, gm4));
-                    continue;
-                }
-                if ((indv & 1) || (indu & 1)) continue;  // zero-inserted tap
-                const unsigned ci = (unsigned)(indv >> 1) + (unsigned)(indu >> 1) * Rc;
-                du = fm(gm4, mul(2.f, cs.du[ci]), du);
-                dv = fm(gm4, mul(2.f, cs.dv[ci]), dv);
-                dw = fm(gm4, cs.dw[ci], dw);
-                pd = fm(gm4, cs.pd[ci], pd);
-                puu = fm(gm4, cs.puu[ci], puu);
-                puv = fm(gm4, cs.puv[ci], puv);
-                pvu = fm(gm4, cs.pvu[ci], pvu);
-                pvv = fm(gm4, cs.pvv[ci], pvv);
-                pwu = fm(gm4, cs.pwu[ci], pwu);
-                pwv = fm(gm4, cs.pwv[ci], pwv);
+    for (int k = -2; k < 3; k++)
+#pragma unroll
+        for (int l = -2; l < 3; l++) {
+            const int indv = (int)v + k, indu = (int)u + l;
+            const float gm4 = mul(4.f, gmask(k, l));
+            if ((indv < 0) || (indv >= (int)R) || (indu < 0) || (indu >= (int)C)) {
+                acu_weight = sub(acu_weight, mul(0.25f, gm4));
+                continue;
             }
-        if (!inner) {
-            const float inv_acu_weight = fdividef(1.f, acu_weight);
-            du = mul(du, inv_acu_weight);
-            dv = mul(dv, inv_acu_weight);
-            dw = mul(dw, inv_acu_weight);
-            pd = mul(pd, inv_acu_weight);
-            puu = mul(puu, inv_acu_weight);
-            puv = mul(puv, inv_acu_weight);
-            pvu = mul(pvu, inv_acu_weight);
-            pvv = mul(pvv, inv_acu_weight);
-            pwu = mul(pwu, inv_acu_weight);
-            pwv = mul(pwv, inv_acu_weight);
+            if ((indv & 1) || (indu & 1)) continue;  // zero-inserted tap
+            const unsigned ci = (unsigned)(indv >> 1) + (unsigned)(indu >> 1) * Rc;
+            acc[0] = fm(gm4, mul(2.f, cs.du[ci]), acc[0]);
+            acc[1] = fm(gm4, mul(2.f, cs.dv[ci]), acc[1]);
+            acc[2] = fm(gm4, cs.dw[ci], acc[2]);
+            acc[3] = fm(gm4, cs.pd[ci], acc[3]);
+            acc[4] = fm(gm4, cs.puu[ci], acc[4]);
+            acc[5] = fm(gm4, cs.puv[ci], acc[5]);
+            acc[6] = fm(gm4, cs.pvu[ci], acc[6]);
+            acc[7] = fm(gm4, cs.pvv[ci], acc[7]);
+            acc[8] = fm(gm4, cs.pwu[ci], acc[8]);
+            acc[9] = fm(gm4, cs.pwv[ci], acc[9]);
         }
+    if (!inner) {
+        const float inv_acu_weight = fdividef(1.f, acu_weight);
+#pragma unroll
+        for (int q = 0; q < 10; ++q) acc[q] = mul(acc[q], inv_acu_weight);
     }
-    L.du_prev[index] = du;
-    L.dv_prev[index] = dv;
+}
+
+// assignZeros (pdflow_cudalib.cu:439-455) with the upsampled solution acc
+// (du dv dw pd puu puv pvu pvv pwu pwv, zero at the coarsest level), then
+// computeRij (:725-779), at one pixel.
+__device__ __forceinline__ void level_init_store(unsigned index, unsigned v, unsigned u, unsigned R, unsigned C,
+                                                 const PyrLevel& o, const PyrLevel& n, const LevelConsts& L,
+                                                 const State& S, const float (&acc)[10])
+{
+    L.du_prev[index] = acc[0];
+    L.dv_prev[index] = acc[1];
     S.du[index] = 0.f;
     S.dv[index] = 0.f;
-    S.dw[index] = dw;
+    S.dw[index] = acc[2];
     S.dua[index] = 0.f;
     S.dva[index] = 0.f;
-    S.dwa[index] = dw;
-    S.pd[index] = pd;
-    S.puu[index] = puu;
-    S.puv[index] = puv;
-    S.pvu[index] = pvu;
-    S.pvv[index] = pvv;
-    S.pwu[index] = pwu;
-    S.pwv[index] = pwv;
+    S.dwa[index] = acc[2];
+    S.pd[index] = acc[3];
+    S.puu[index] = acc[4];
+    S.puv[index] = acc[5];
+    S.pvu[index] = acc[6];
+    S.pvv[index] = acc[7];
+    S.pwu[index] = acc[8];
+    S.pwv[index] = acc[9];
 
     // computeRij
     float dxu = 0.f, dzu = 0.f, dxu_2 = 0.f, dzu_2 = 0.f, dyv = 0.f, dzv = 0.f, dyv_2 = 0.f, dzv_2 = 0.f;
@@ -275,6 +260,111 @@ __global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, P
     L.rj[index] = rfac(dyv, dzv);
     L.ri2[index] = rfac(dxu_2, dzu_2);
     L.rj2[index] = rfac(dyv_2, dzv_2);
+}
+
+// Level set-up, one pixel per thread: the coarsest level (zeros), a warm
+// start's seed (its flow, duals from zero), or the upsampled coarse solution.
+__global__ void k_level_init(LevelGeom g, bool first, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S,
+                             const float* __restrict__ seed)
+{
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
+    cs = at(cs, po);
+    o = at(o, po);
+    n = at(n, po);
+    L = at(L, po);
+    S = at(S, po);
+    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= g.N) return;
+    const unsigned R = g.R, C = g.C;
+    const unsigned v = index % R, u = index / R;
+    float acc[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (seed) {   // warm start: a predicted solution of this level, duals from zero
+        const float* sp = seed + (size_t)blockIdx.y * 3 * g.N;
+        acc[0] = sp[index];
+        acc[1] = sp[g.N + index];
+        acc[2] = sp[2 * g.N + index];
+    } else if (!first) {
+        upsample_px(cs, v, u, R, C, acc);
+    }
+    level_init_store(index, v, u, R, C, o, n, L, S, acc);
+}
+
+// Level set-up with the upsampled coarse solution, one vertical pixel pair
+// (rows 2a, 2a+1 of column u) per thread.  In a pair whose pixels are both
+// inner, the even row's taps with a coarse sample are rows -2, 0, +2 and the
+// odd row's -1, +1, and the column's parity fixes the columns (-2, 0, +2 or
+// -1, +1): both pixels read the same 3 x 3 (or 3 x 2) coarse neighbourhood,
+// loaded once per plane, and accumulate their taps in the reference's order.
+// Border pairs take the per-pixel gather.  Same bits as k_level_init.
+__global__ void k_level_init_pairs(LevelGeom g, LevelSol cs, PyrLevel o, PyrLevel n, LevelConsts L, State S)
+{
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
+    cs = at(cs, po);
+    o = at(o, po);
+    n = at(n, po);
+    L = at(L, po);
+    S = at(S, po);
+    const unsigned R = g.R, C = g.C, Rc = R / 2;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Rc * C) return;
+    const unsigned a = t % Rc, u = t / Rc, v0 = 2 * a, index0 = v0 + u * R;
+    float acc0[10], acc1[10];
+    if (a >= 1 && v0 + 3 < R && u > 1 && u + 2 < C) {
+        const unsigned b = u >> 1;
+        const float* planes[10] = {cs.du, cs.dv, cs.dw, cs.pd, cs.puu, cs.puv, cs.pvu, cs.pvv, cs.pwu, cs.pwv};
+        if ((u & 1u) == 0) {   // column taps -2, 0, +2: coarse columns b-1, b, b+1
+#pragma unroll
+            for (int q = 0; q < 10; ++q) {
+                float c[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) {
+                        const float x = planes[q][(a - 1 + r) + (b - 1 + e) * Rc];
+                        c[r][e] = q < 2 ? mul(2.f, x) : x;
+                    }
+                float x0 = 0.f, x1 = 0.f;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)   // even row: row taps -2, 0, +2 = coarse rows a-1, a, a+1
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) x0 = fm(mul(4.f, gmask(2 * r - 2, 2 * e - 2)), c[r][e], x0);
+#pragma unroll
+                for (int r = 1; r < 3; ++r)   // odd row: row taps -1, +1 = coarse rows a, a+1
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) x1 = fm(mul(4.f, gmask(2 * r - 3, 2 * e - 2)), c[r][e], x1);
+                acc0[q] = x0;
+                acc1[q] = x1;
+            }
+        } else {   // column taps -1, +1: coarse columns b, b+1
+#pragma unroll
+            for (int q = 0; q < 10; ++q) {
+                float c[3][2];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const float x = planes[q][(a - 1 + r) + (b + e) * Rc];
+                        c[r][e] = q < 2 ? mul(2.f, x) : x;
+                    }
+                float x0 = 0.f, x1 = 0.f;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) x0 = fm(mul(4.f, gmask(2 * r - 2, 2 * e - 1)), c[r][e], x0);
+#pragma unroll
+                for (int r = 1; r < 3; ++r)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) x1 = fm(mul(4.f, gmask(2 * r - 3, 2 * e - 1)), c[r][e], x1);
+                acc0[q] = x0;
+                acc1[q] = x1;
+            }
+        }
+    } else {
+        upsample_px(cs, v0, u, R, C, acc0);
+        upsample_px(cs, v0 + 1, u, R, C, acc1);
+    }
+    level_init_store(index0, v0, u, R, C, o, n, L, S, acc0);
+    level_init_store(index0 + 1, v0 + 1, u, R, C, o, n, L, S, acc1);
 }
 
 // computeImGradients (pdflow_cudalib.cu:574-627) on the new frame.
@@ -753,7 +843,10 @@ static dim3 level_grid(const LevelGeom& g) { return dim3(blocks_for(g.N), g.pair
 cudaError_t launch_level_init(LevelGeom g, bool first, LevelSol coarse, PyrLevel old_l, PyrLevel new_l,
                               LevelConsts L, State S, cudaStream_t st, const float* seed)
 {
-    k_level_init<<<level_grid(g), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S, seed);
+    if (!first && !seed && g.R % 2 == 0)
+        k_level_init_pairs<<<dim3(blocks_for(g.N / 2), g.pairs), kBlock, 0, st>>>(g, coarse, old_l, new_l, L, S);
+    else
+        k_level_init<<<level_grid(g), kBlock, 0, st>>>(g, first, coarse, old_l, new_l, L, S, seed);
     return cudaGetLastError();
 }
 
