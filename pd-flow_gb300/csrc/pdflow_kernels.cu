@@ -422,13 +422,15 @@ __global__ void k_warp_steps(LevelGeom g, PyrLevel o, PyrLevel n, LevelConsts L,
     const unsigned v = index % R, u = index / R;
     const float ind_uf = add(float(u), L.du_prev[index]);
     const float ind_vf = add(float(v), L.dv_prev[index]);
-    const float dct = sub(interp(n.col, R, C, ind_uf, ind_vf), o.col[index]);
-    const float dcu = interp(L.dcu_aux, R, C, ind_uf, ind_vf);
-    const float dcv = interp(L.dcv_aux, R, C, ind_uf, ind_vf);
-    const float wz = interp_depth(n.dep, R, C, ind_uf, ind_vf);
+    // the five plain interpolations at one position share their case analysis
+    const Bilin b = bilin(R, C, ind_uf, ind_vf);
+    const float* const mats[5] = {n.col, L.dcu_aux, L.dcv_aux, L.ddu_aux, L.ddv_aux};
+    float w5[5];
+    bilin_blend_n<5>(mats, R, b, w5);
+    const float dct = sub(w5[0], o.col[index]);
+    const float dcu = w5[1], dcv = w5[2], ddu = w5[3], ddv = w5[4];
+    const float wz = interp_depth_at(n.dep, R, b);
     const float ddt = (wz > 0.f) ? sub(wz, o.dep[index]) : 0.f;
-    const float ddu = interp(L.ddu_aux, R, C, ind_uf, ind_vf);
-    const float ddv = interp(L.ddv_aux, R, C, ind_uf, ind_vf);
     L.dct[index] = dct;
     L.dcu[index] = dcu;
     L.dcv[index] = dcv;

@@ -115,18 +115,41 @@ __device__ __forceinline__ float bilin_blend(const float* __restrict__ mat, unsi
     return fm(sub(b.iv, float(b.fv)), val_sup_v, mul(sub(float(b.sv), b.iv), val_inf_v));
 }
 
-__device__ __forceinline__ float interp(const float* __restrict__ mat, unsigned R, unsigned C, float ind_u,
-                                        float ind_v)
+// bilin_blend of N matrices at the same position: one case analysis, each
+// matrix blended with the same expressions (the same bits as N calls).
+template <int N>
+__device__ __forceinline__ void bilin_blend_n(const float* const (&mat)[N], unsigned R, const Bilin& b, float (&out)[N])
 {
-    return bilin_blend(mat, R, bilin(R, C, ind_u, ind_v));
+    if ((b.su == b.fu) && (b.sv == b.fv)) {
+        const long i = lrintf(fm(float(R), b.iu, b.iv));
+#pragma unroll
+        for (int m = 0; m < N; ++m) out[m] = mat[m][i];
+    } else if (b.su == b.fu) {
+        const long cu = lrintf(b.iu);
+        const float wl = sub(float(b.sv), b.iv), wr = sub(b.iv, float(b.fv));
+#pragma unroll
+        for (int m = 0; m < N; ++m) out[m] = fm(wl, mat[m][b.fv + R * cu], mul(wr, mat[m][b.sv + R * cu]));
+    } else if (b.sv == b.fv) {
+        const long cv = lrintf(b.iv);
+        const float wl = sub(float(b.su), b.iu), wr = sub(b.iu, float(b.fu));
+#pragma unroll
+        for (int m = 0; m < N; ++m) out[m] = fm(wl, mat[m][cv + R * b.fu], mul(wr, mat[m][cv + R * b.su]));
+    } else {
+        const float A = sub(float(b.su), b.iu), B = sub(b.iu, float(b.fu));
+        const float wv = sub(b.iv, float(b.fv)), wf = sub(float(b.sv), b.iv);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+            const float val_sup_v = fm(A, mat[m][b.sv + R * b.fu], mul(B, mat[m][b.sv + R * b.su]));
+            const float val_inf_v = fm(A, mat[m][b.fv + R * b.fu], mul(B, mat[m][b.fv + R * b.su]));
+            out[m] = fm(wv, val_sup_v, mul(wf, val_inf_v));
+        }
+    }
 }
 
 // interpolatePixelDepth (pdflow_cudalib.cu:684-721): nearest sample
 // (round-half-even) when any of the four taps is a hole.
-__device__ __forceinline__ float interp_depth(const float* __restrict__ mat, unsigned R, unsigned C, float ind_u,
-                                              float ind_v)
+__device__ __forceinline__ float interp_depth_at(const float* __restrict__ mat, unsigned R, const Bilin& b)
 {
-    const Bilin b = bilin(R, C, ind_u, ind_v);
     if ((mat[b.sv + R * b.su] == 0.f) || (mat[b.sv + R * b.fu] == 0.f) || (mat[b.fv + R * b.su] == 0.f) ||
         (mat[b.fv + R * b.fu] == 0.f)) {
         const unsigned rind_u = __float2int_rn(b.iu);
