@@ -80,6 +80,27 @@ int pdflow_server_wait(pdflow_server* srv, unsigned long long request_id, int ti
 
 int pdflow_server_get_stats(pdflow_server* srv, pdflow_server_stats* stats);
 
+/* A camera stream's recorded frames for pdflow_server_replay: frame k is
+ * intensity[k] / depth[k] (host, row-major, the stream's size). */
+typedef struct pdflow_replay_stream {
+    unsigned stream_id;
+    unsigned frames;
+    const uint8_t* const* intensity;
+    const uint16_t* const* depth;
+} pdflow_replay_stream;
+
+/* Load generator (no counterpart in the reference): replays the streams'
+ * frames with Poisson arrivals, each stream's gaps exponential of mean
+ * 1 / rate_hz (seeded), from a generator thread that sleeps until each
+ * arrival and submits it, then waits for every request.  info[m] and
+ * late_ms[m] (how late submission m was against its schedule) are filled in
+ * submission order, *count of them (at most `capacity`: PDFLOW_ERR_ARG when
+ * the streams hold more frames).  An error from a submission ends the
+ * replay after waiting for the requests already submitted. */
+int pdflow_server_replay(pdflow_server* srv, const pdflow_replay_stream* streams, unsigned n_streams, double rate_hz,
+                         unsigned long long seed, pdflow_request_info* info, double* late_ms, unsigned capacity,
+                         unsigned* count);
+
 #ifdef __cplusplus
 }
 #endif

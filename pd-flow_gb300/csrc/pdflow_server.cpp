@@ -15,6 +15,8 @@
 #include <memory>
 #include <mutex>
 #include <new>
+#include <queue>
+#include <random>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -363,16 +365,28 @@ int pdflow_server_submit(pdflow_server* s, unsigned id, const uint8_t* intensity
     Request* r = new (std::nothrow) Request();
     if (!r) return fail(PDFLOW_ERR_OOM, "host allocation");
     r->t_submit = Clock::now();
+    size_t img = 0;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (id < s->streams.size() && s->streams[id].open) {
+            const Lane* L = s->lanes[s->streams[id].lane].get();
+            img = size_t(L->width) * L->height;
+        }
+    }
+    if (img == 0) {
+        delete r;
+        return fail(PDFLOW_ERR_ARG, "no such stream");
+    }
+    // the frame is copied without the server's lock (the workers keep going)
+    r->inten.assign(intensity, intensity + img);
+    r->depth.assign(depth, depth + img);
     std::unique_lock<std::mutex> lk(s->mu);
-    if (id >= s->streams.size() || !s->streams[id].open) {
+    if (id >= s->streams.size() || !s->streams[id].open) {   // closed meanwhile
         delete r;
         return fail(PDFLOW_ERR_ARG, "no such stream");
     }
     Stream& st = s->streams[id];
     Lane* L = s->lanes[st.lane].get();
-    const size_t img = size_t(L->width) * L->height;
-    r->inten.assign(intensity, intensity + img);
-    r->depth.assign(depth, depth + img);
     r->id = s->next_id++;
     r->stream = id;
     r->slot = st.slot;
@@ -421,6 +435,51 @@ int pdflow_server_wait(pdflow_server* s, unsigned long long request_id, int time
     s->requests.erase(it);
     delete r;
     return PDFLOW_OK;
+}
+
+int pdflow_server_replay(pdflow_server* s, const pdflow_replay_stream* streams, unsigned n_streams, double rate_hz,
+                         unsigned long long seed, pdflow_request_info* info, double* late_ms, unsigned capacity,
+                         unsigned* count)
+{
+    if (!s || !streams || !info || !late_ms || !count || !(rate_hz > 0.0)) return fail(PDFLOW_ERR_ARG, "bad argument");
+    size_t total = 0;
+    for (unsigned i = 0; i < n_streams; ++i) {
+        if (streams[i].frames && (!streams[i].intensity || !streams[i].depth)) return fail(PDFLOW_ERR_ARG, "null frames");
+        total += streams[i].frames;
+    }
+    if (total > capacity) return fail(PDFLOW_ERR_ARG, "more frames than result slots");
+    struct Arrival {
+        double t;   // seconds after the start
+        unsigned stream, frame;
+        bool operator>(const Arrival& o) const { return t > o.t; }
+    };
+    std::mt19937_64 rng(seed);
+    std::exponential_distribution<double> gap(rate_hz);
+    std::priority_queue<Arrival, std::vector<Arrival>, std::greater<Arrival>> due;
+    for (unsigned i = 0; i < n_streams; ++i)
+        if (streams[i].frames) due.push({gap(rng), i, 0});
+    std::vector<unsigned long long> ids;
+    ids.reserve(total);
+    int rc = PDFLOW_OK;
+    const auto t0 = Clock::now();
+    while (!due.empty()) {
+        const Arrival a = due.top();
+        due.pop();
+        std::this_thread::sleep_until(t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(a.t)));
+        const pdflow_replay_stream& st = streams[a.stream];
+        unsigned long long id = 0;
+        late_ms[ids.size()] = std::chrono::duration<double, std::milli>(Clock::now() - t0).count() - a.t * 1e3;
+        rc = pdflow_server_submit(s, st.stream_id, st.intensity[a.frame], st.depth[a.frame], &id);
+        if (rc != PDFLOW_OK) break;
+        ids.push_back(id);
+        if (a.frame + 1 < st.frames) due.push({a.t + gap(rng), a.stream, a.frame + 1});
+    }
+    for (size_t m = 0; m < ids.size(); ++m) {
+        const int w = pdflow_server_wait(s, ids[m], -1, &info[m], nullptr, nullptr, nullptr);
+        if (w != PDFLOW_OK && rc == PDFLOW_OK) rc = w;
+    }
+    *count = unsigned(ids.size());
+    return rc;
 }
 
 int pdflow_server_get_stats(pdflow_server* s, pdflow_server_stats* out)

@@ -92,6 +92,12 @@ class RequestInfo(ctypes.Structure):
                 ("done_ms", ctypes.c_double)]
 
 
+class ReplayStream(ctypes.Structure):
+    """pdflow_replay_stream (include/pdflow_server.h)."""
+    _fields_ = [("stream_id", ctypes.c_uint), ("frames", ctypes.c_uint),
+                ("intensity", ctypes.POINTER(ctypes.c_void_p)), ("depth", ctypes.POINTER(ctypes.c_void_p))]
+
+
 class ServerStats(ctypes.Structure):
     """pdflow_server_stats (include/pdflow_server.h)."""
     _fields_ = [("lanes", ctypes.c_uint), ("streams", ctypes.c_uint), ("submitted", ctypes.c_ulonglong),
@@ -174,6 +180,9 @@ _SIGNATURES = {
     "pdflow_server_wait": (ctypes.c_int, [vp, ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(RequestInfo), vp, vp,
                                           vp]),
     "pdflow_server_get_stats": (ctypes.c_int, [vp, ctypes.POINTER(ServerStats)]),
+    "pdflow_server_replay": (ctypes.c_int, [vp, ctypes.POINTER(ReplayStream), u32, ctypes.c_double, ctypes.c_ulonglong,
+                                            ctypes.POINTER(RequestInfo), ctypes.POINTER(ctypes.c_double), u32,
+                                            ctypes.POINTER(ctypes.c_uint)]),
     "pdflow_seed_level_inputs": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_seed_level_labels": (ctypes.c_int, [vp, u32, vp]),
     "pdflow_set_level_form": (ctypes.c_int, [vp, u32, ctypes.c_int, u32]),

@@ -5,7 +5,9 @@ multi-camera workload for it.
 frames are submitted as they arrive and results are collected with their
 timings.  `simulate` drives a server with camera streams whose frames arrive
 as Poisson processes (default 30 Hz each) and reports latency percentiles and
-aggregate throughput.
+aggregate throughput; for the C server the arrivals come from its native load
+generator (pdflow_server_replay: a C++ thread that sleeps until each arrival),
+for other servers (tests) from a Python loop.
 """
 from __future__ import annotations
 
@@ -15,7 +17,7 @@ import time
 
 import numpy as np
 
-from ._lib import (RequestInfo, ServerConfig, ServerStats, _ptr, check, load)
+from ._lib import (ReplayStream, RequestInfo, ServerConfig, ServerStats, _ptr, check, load)
 
 
 class Server:
@@ -66,6 +68,27 @@ class Server:
         d = {k: getattr(info, k) for k, _ in RequestInfo._fields_}
         return d, (flows if (want_flow and info.has_flow) else None)
 
+    def replay(self, sids, streams, rate_hz: float, seed: int):
+        """pdflow_server_replay: streams[i] = (width, height, frames) for the
+        opened stream sids[i]; returns (infos in submission order, lateness ms)."""
+        keep, rs = [], (ReplayStream * len(sids))()
+        for i, (sid, (_, _, frames)) in enumerate(zip(sids, streams)):
+            h, w = self._shape[sid]
+            arrs = [(np.ascontiguousarray(a, np.uint8), np.ascontiguousarray(z, np.uint16)) for a, z in frames]
+            if any(a.shape != (h, w) or z.shape != (h, w) for a, z in arrs):
+                raise ValueError("frame size does not match the stream")
+            ip = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a, _ in arrs])
+            dp = (ctypes.c_void_p * len(arrs))(*[z.ctypes.data for _, z in arrs])
+            keep += [arrs, ip, dp]
+            rs[i] = ReplayStream(sid, len(arrs), ctypes.cast(ip, ctypes.POINTER(ctypes.c_void_p)),
+                                 ctypes.cast(dp, ctypes.POINTER(ctypes.c_void_p)))
+        total = sum(len(f) for _, _, f in streams)
+        infos, late, count = (RequestInfo * total)(), (ctypes.c_double * total)(), ctypes.c_uint()
+        check(load().pdflow_server_replay(self._h, rs, len(sids), rate_hz, seed, infos, late, total,
+                                          ctypes.byref(count)), "pdflow_server_replay")
+        out = [{k: getattr(infos[m], k) for k, _ in RequestInfo._fields_} for m in range(count.value)]
+        return out, [late[m] for m in range(count.value)]
+
     def stats(self) -> dict:
         st = ServerStats()
         check(load().pdflow_server_get_stats(self._h, ctypes.byref(st)), "pdflow_server_get_stats")
@@ -86,34 +109,39 @@ class Server:
 def simulate(server: Server, streams, rate_hz: float = 30.0, seed: int = 0, want_flow: bool = False):
     """streams: list of (width, height, frames) with frames a list of
     (intensity, depth) numpy pairs.  Each stream's frames arrive as a Poisson
-    process of rate `rate_hz` (exponential gaps).  Returns per-request infos
-    and a summary: p50 / p99 latency of the frames that produced a flow,
-    aggregate flows per second over the run, batch sizes, and how late the
-    submissions ran against their scheduled arrival times (a late load
-    generator bunches arrivals into bursts)."""
-    rng = np.random.default_rng(seed)
+    process of rate `rate_hz` (exponential gaps; for a `Server`, generated and
+    submitted by its native load generator unless flows are wanted back).
+    Returns per-request infos and a summary: p50 / p99 latency of the frames
+    that produced a flow, aggregate flows per second over the run, batch
+    sizes, and how late the submissions ran against their scheduled arrival
+    times (a late load generator bunches arrivals into bursts)."""
     sids = [server.open_stream(w, h) for w, h, _ in streams]
-    heap = []
     t0 = time.perf_counter()
-    for j, (_, _, frames) in enumerate(streams):
-        heapq.heappush(heap, (rng.exponential(1.0 / rate_hz), j, 0))
-    pending, late = [], []
-    while heap:
-        t_arr, j, k = heapq.heappop(heap)
-        now = time.perf_counter() - t0
-        if t_arr > now:
-            time.sleep(t_arr - now)
-        late.append((time.perf_counter() - t0 - t_arr) * 1e3)
-        frames = streams[j][2]
-        rid = server.submit(sids[j], *frames[k])
-        pending.append((rid, sids[j]))
-        if k + 1 < len(frames):
-            heapq.heappush(heap, (t_arr + rng.exponential(1.0 / rate_hz), j, k + 1))
-    infos, outs = [], []
-    for rid, sid in pending:
-        info, flow = server.wait(rid, sid, want_flow=want_flow)
-        infos.append(info)
-        outs.append(flow)
+    if isinstance(server, Server) and not want_flow:
+        infos, late = server.replay(sids, streams, rate_hz, seed)
+        outs = [None] * len(infos)
+    else:
+        rng = np.random.default_rng(seed)
+        heap = []
+        for j, (_, _, frames) in enumerate(streams):
+            heapq.heappush(heap, (rng.exponential(1.0 / rate_hz), j, 0))
+        pending, late = [], []
+        while heap:
+            t_arr, j, k = heapq.heappop(heap)
+            now = time.perf_counter() - t0
+            if t_arr > now:
+                time.sleep(t_arr - now)
+            late.append((time.perf_counter() - t0 - t_arr) * 1e3)
+            frames = streams[j][2]
+            rid = server.submit(sids[j], *frames[k])
+            pending.append((rid, sids[j]))
+            if k + 1 < len(frames):
+                heapq.heappush(heap, (t_arr + rng.exponential(1.0 / rate_hz), j, k + 1))
+        infos, outs = [], []
+        for rid, sid in pending:
+            info, flow = server.wait(rid, sid, want_flow=want_flow)
+            infos.append(info)
+            outs.append(flow)
     wall = time.perf_counter() - t0
     lat = np.array([i["done_ms"] - i["submit_ms"] for i in infos if i["has_flow"]])
     flows = int(sum(1 for i in infos if i["has_flow"]))

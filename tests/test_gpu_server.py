@@ -78,3 +78,22 @@ def test_admission_is_bounded_by_the_device_budget(built_lib):
         srv.open_stream(320, 240)             # would need a second lane
     assert e.value.code == ERR_OOM
     srv.close()
+
+
+def test_native_replay_submits_every_frame_on_schedule(built_lib):
+    """pdflow_server_replay: the native load generator submits each stream's
+    frames in order at Poisson arrival times and returns every request."""
+    from pdflow.serving import simulate
+    srv = Server(device_budget_bytes=64 << 30, slots_per_lane=4)
+    streams = [(320, 240, stream_frames(400 + j, False, 5)) for j in range(3)] + \
+              [(640, 480, stream_frames(410, True, 4))]
+    infos, _, summary = simulate(srv, streams, rate_hz=60.0, seed=7)
+    srv.close()
+    assert summary["requests"] == 19 and summary["flows"] == 15 and summary["errors"] == 0
+    per_stream = {}
+    for i in infos:
+        per_stream.setdefault(i["stream_id"], []).append(i["frame_index"])
+    assert sorted(len(v) for v in per_stream.values()) == [4, 5, 5, 5]
+    assert all(v == list(range(len(v))) for v in per_stream.values())
+    assert all(i["done_ms"] >= i["start_ms"] >= i["submit_ms"] for i in infos)
+    assert summary["arrival_lateness_p99_ms"] < 50.0
