@@ -30,8 +30,9 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
  * right and hands each region's last exact column's exchange values to the
  * next one, so that only a right halo is recomputed (28 of 32 columns exact
  * at 4 iterations per launch); levels with fewer bands than SMs run 8
- * instead; 9 = as 8 with 16x16 interiors and a halo of 8 (up to 8 iterations
- * per launch); 8 = every
+ * instead, or 9 where all of the level's 16x16 tiles fit in one round of
+ * CTAs (a single pair's 60x80 and 120x160 levels); 9 = as 8 with 16x16
+ * interiors and a halo of 8 (up to 8 iterations per launch); 8 = every
  * level of a batch (more than one pair), and a single pair's levels above 300
  * pixels, as temporally blocked 24x24 tiles (halo 4, up to 4 iterations per
  * launch) walked by one persistent CTA per SM, each tile's state and

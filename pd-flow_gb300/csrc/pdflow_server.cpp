@@ -51,6 +51,7 @@ struct Lane {
     pdflow_net* net = nullptr;
     std::vector<int> slot_stream;           // stream id per slot, -1 = free
     std::deque<Request*> pending;
+    std::condition_variable cv;             // the lane's worker waits here for pending frames
     std::thread worker;
     uint8_t* st_i = nullptr;                // pinned staging [slots][h][w]
     uint16_t* st_z = nullptr;
@@ -72,7 +73,7 @@ struct pdflow_server {
     std::vector<float> params;
     Clock::time_point t0;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_done;
     int device = 0;
     std::vector<std::unique_ptr<Lane>> lanes;
     std::vector<Stream> streams;
@@ -141,7 +142,8 @@ void run_batch(pdflow_server* srv, Lane* L, std::vector<Request*>& batch)
         rc = pdflow_synchronize(L->solver);
     }
     const auto t_done = Clock::now();
-    std::lock_guard<std::mutex> lk(srv->mu);
+    // results into the requests and their frames freed before the server's
+    // lock: nothing else touches a request of this batch until it is done
     for (unsigned j = 0; j < m && rc == PDFLOW_OK; ++j) {
         Request* r = batch[solve_idx[j]];
         r->dx.assign(L->out + j * N, L->out + (j + 1) * N);
@@ -150,15 +152,18 @@ void run_batch(pdflow_server* srv, Lane* L, std::vector<Request*>& batch)
         r->has_flow = true;
     }
     for (Request* r : batch) {
+        r->inten.clear();
+        r->inten.shrink_to_fit();
+        r->depth.clear();
+        r->depth.shrink_to_fit();
+    }
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (Request* r : batch) {
         r->status = rc;
         r->done = true;
         r->t_done = t_done;
         r->batch_pairs = m;
         r->batch_fallbacks = rep.fallbacks;
-        r->inten.clear();
-        r->inten.shrink_to_fit();
-        r->depth.clear();
-        r->depth.shrink_to_fit();
         srv->streams[r->stream].inflight--;
     }
     srv->stats.completed += n;
@@ -175,7 +180,7 @@ void lane_worker(pdflow_server* srv, Lane* L)
         std::vector<Request*> batch;
         {
             std::unique_lock<std::mutex> lk(srv->mu);
-            srv->cv_work.wait(lk, [&] { return srv->stop || !L->pending.empty(); });
+            L->cv.wait(lk, [&] { return srv->stop || !L->pending.empty(); });
             if (L->pending.empty()) return;   // stop requested and nothing left
             // the oldest pending frame of each stream, in arrival order
             std::vector<unsigned char> taken(srv->streams.size(), 0);
@@ -297,7 +302,7 @@ int pdflow_server_destroy(pdflow_server* s)
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
     }
-    s->cv_work.notify_all();
+    for (auto& L : s->lanes) L->cv.notify_all();
     for (auto& L : s->lanes)
         if (L->worker.joinable()) L->worker.join();
     for (auto& L : s->lanes) destroy_lane(L.get());
@@ -397,7 +402,7 @@ int pdflow_server_submit(pdflow_server* s, unsigned id, const uint8_t* intensity
     s->stats.submitted++;
     if (request_id) *request_id = r->id;
     lk.unlock();
-    s->cv_work.notify_all();
+    L->cv.notify_one();   // only this lane's worker has new work
     return PDFLOW_OK;
 }
 
@@ -426,13 +431,14 @@ int pdflow_server_wait(pdflow_server* s, unsigned long long request_id, int time
         info->start_ms = ms_since(s, r->t_start);
         info->done_ms = ms_since(s, r->t_done);
     }
+    s->requests.erase(it);
+    lk.unlock();   // the request is ours now: its flow is copied without the lock
     if (r->has_flow) {
         const size_t N = r->dx.size();
         if (dx) std::memcpy(dx, r->dx.data(), N * 4);
         if (dy) std::memcpy(dy, r->dy.data(), N * 4);
         if (dz) std::memcpy(dz, r->dz.data(), N * 4);
     }
-    s->requests.erase(it);
     delete r;
     return PDFLOW_OK;
 }

@@ -214,12 +214,16 @@ static bool level_runs_tiles(const pdflow_solver* s, const LevelGeom& g, unsigne
 // The level's iteration form: its autotuned or hand-set form, else the
 // handle's.  By default the strips (form 10) run only where the level has a
 // strip (a pair's 24-row band) for every SM; smaller levels run the streamed
-// tiles (form 8), which deal fewer pixels to every SM.
+// tiles (form 8), which deal fewer pixels to every SM, and levels whose 16x16
+// tiles all fit in one round of CTAs the deep tiles (form 9: twice the
+// iterations per launch where the launches are latency-bound, as the
+// autotuner finds for a single pair's 60x80 and 120x160 levels).
 static int level_form(const pdflow_solver* s, const LevelGeom& g, unsigned pairs, unsigned level)
 {
     const int forced = level < 8 ? s->level_form[level] : -1;
     if (forced >= 0) return forced;
-    if (s->iter_form == 10 && pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms)) return 8;
+    if (s->iter_form == 10 && pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms))
+        return pairs * ((g.R + 15u) / 16u) * ((g.C + 15u) / 16u) <= unsigned(s->num_sms) ? 9 : 8;
     return s->iter_form;
 }
 
