@@ -42,7 +42,7 @@ struct pdflow_solver {
     unsigned* flags = nullptr;           // per-CTA progress counters of the grid-form iteration
     unsigned* status = nullptr;          // device status word (0 = ok)
     int num_sms = 0;
-    int iter_form = 10;                  // 10 = streamed strips (levels with a strip per SM; others form 8),
+    int iter_form = 10;                  // 10 = streamed strips (levels with a strip per SM; others 9 or 8),
                                          // 9 = deep streamed tiles,
                                          // 8 = streamed register tiles (persistent, one CTA per SM), 7 = quad
                                          // register tiles, 5 / 4 / 3 = paired tiles 24x24 (two CTAs per SM) / 40x34 / 40x40,

@@ -1,5 +1,5 @@
 // Persistent, register-resident tile iterations ("streamed tiles", iteration
-// form 8).
+// forms 8 and 9; the strips of form 10 below).
 //
 // One CTA per SM walks a list of tiles (every 24 x 24 interior of every pair
 // of the launch, 4-pixel halo: 32 x 32 regions, as in pdflow_tiles2.cu).  A
