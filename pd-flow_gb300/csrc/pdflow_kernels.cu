@@ -565,13 +565,17 @@ __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* dep
 // reference does, and the bracketing samples are interpolated; the result and
 // the selected index are the reference's bit for bit.  Every index is a
 // compile-time constant: nothing spills.
-__device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned n, float med_or_neg,
-                                         float* total, int32_t* cont_out)
+__device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned present, unsigned n,
+                                         float med_or_neg, float* total, int32_t* cont_out)
 {
+    // the samples in tap order, a missing one (bit clear in `present`) as +inf
+    // of weight 0: the stable sort keeps the present samples in their order
+    // and puts the missing ones after them, so its first n entries are those
+    // of the reference's sort of the n present samples
     float sf[9], sw[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
-        const bool in = (unsigned)i < n;
+        const bool in = (present >> i) & 1u;
         sf[i] = in ? f[i] : INFINITY;
         sw[i] = in ? w[i] : 0.f;
     }
@@ -634,35 +638,32 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     const float depth_old = o.dep[index];
     float ru, rv, rw;
     if (depth_old > 0.f) {
+        // the nine taps in the reference's order (row offset, then column);
+        // taps outside the image are marked missing (median9)
         float fu[9], fv[9], fw[9], wt[9];
-        unsigned n = 0;
+        unsigned present = 0;
 #pragma unroll
         for (int k = -1; k < 2; k++)
 #pragma unroll
             for (int l = -1; l < 2; l++) {
+                const int q = 3 * (k + 1) + (l + 1);
                 const int indr = (int)v + k, indc = (int)u + l;
                 const bool in = (indr >= 0) && (indr < (int)R) && (indc >= 0) && (indc < (int)C);
                 const int j = in ? (int)index + l * (int)R + k : (int)index;
-                const float pres = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
-                                          : median_weight(depth_old, o.dep[j], L.ddt[j]);
-                const float a = S.du[j], b = S.dv[j], c = S.dw[j];
-                // compact the present samples to the front, in the reference's order
-#pragma unroll
-                for (int q = 0; q < 9; ++q)
-                    if (in && (unsigned)q == n) {
-                        fu[q] = a; fv[q] = b; fw[q] = c; wt[q] = pres;
-                    }
-                if (in) ++n;
+                wt[q] = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
+                               : median_weight(depth_old, o.dep[j], L.ddt[j]);
+                fu[q] = S.du[j];
+                fv[q] = S.dv[j];
+                fw[q] = S.dw[j];
+                present |= (in ? 1u : 0u) << q;
             }
-#pragma unroll
-        for (int q = 0; q < 9; ++q)
-            if ((unsigned)q >= n) { fu[q] = 0.f; fv[q] = 0.f; fw[q] = 0.f; wt[q] = 0.f; }
+        const unsigned n = __popc(present);
         float tot;
         int32_t c0, c1, c2;
-        ru = median9(fu, wt, n, -1.f, &tot, &c0);
+        ru = median9(fu, wt, present, n, -1.f, &tot, &c0);
         const float pres_med = mul(0.5f, tot);   // half of u's total, for all three (:1097)
-        rv = median9(fv, wt, n, pres_med, &tot, &c1);
-        rw = median9(fw, wt, n, pres_med, &tot, &c2);
+        rv = median9(fv, wt, present, n, pres_med, &tot, &c1);
+        rw = median9(fw, wt, present, n, pres_med, &tot, &c2);
         if (sel) { sel[index] = c0; sel[g.N + index] = c1; sel[2 * g.N + index] = c2; }
     } else {
         ru = S.du[index];
