@@ -72,6 +72,11 @@ cudaError_t prepare_quads();
 // words: [0] the status word, [2] and [3] the strip walk's unit counters
 // (zero between launches; the kernel leaves them so).
 enum class StreamLayout { Tiles24, Tiles16, Strips };
+// Whether a level can run register-resident tile form `form` (7-10): the
+// quad tiles and the strips need quads_eligible (tensor copies); the
+// streamed tiles (8, 9) also run on direct loads where the rows are even.
+bool stream_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst, int form);
+bool stream_direct_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst);
 inline StreamLayout stream_layout(int form)
 {
     return form == 9 ? StreamLayout::Tiles16 : (form == 10 ? StreamLayout::Strips : StreamLayout::Tiles24);

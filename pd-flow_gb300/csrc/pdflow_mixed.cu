@@ -53,15 +53,17 @@ unsigned step_kk(const pdflow_solver* s, unsigned i, int form)
 }
 
 // Tile form at step i: the autotuned choice, else the handle's paired form
-// (forms 7-10 need rows % 4 == 0, levels 15x20 and 30x40 run form 5; by
-// default the strips, form 10, need a strip per SM, else form 8 runs, or
-// form 9 where the 16x16 tiles fit in one round of CTAs).
+// (forms 7 and 10 need rows % 4 == 0, forms 8 and 9 even rows; the 15x20
+// level runs form 5; by default the strips, form 10, need a strip per SM and
+// rows % 4 == 0, else form 8 runs, or form 9 where the 16x16 tiles fit in one
+// round of CTAs).
 int step_form(const pdflow_solver* s, unsigned i, const LevelGeom& g)
 {
     int f = s->mixed_form[i] >= 3 ? s->mixed_form[i] : (s->iter_form >= 3 ? s->iter_form : 5);
-    if (s->mixed_form[i] < 3 && f == 10 && g.pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms))
+    if (s->mixed_form[i] < 3 && f == 10 &&
+        (g.pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms) || !stream_eligible(g, s->L, s->S, s->S, 10)))
         f = g.pairs * ((g.R + 15u) / 16u) * ((g.C + 15u) / 16u) <= unsigned(s->num_sms) ? 9 : 8;
-    if (f >= 7 && !quads_eligible(g, s->L, s->S, s->S)) f = 5;
+    if (f >= 7 && !stream_eligible(g, s->L, s->S, s->S, f)) f = 5;
     return f;
 }
 
@@ -245,7 +247,7 @@ int pdflow::mixed_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, p
                 const int form = tune_candidate(idx).form;
                 const unsigned kk = tune_candidate(idx).kk;
                 if (form < 3) continue;                   // mixed steps run tile forms only
-                if (form >= 7 && !quads_eligible(g, s->L, s->S, s->S)) continue;
+                if (form >= 7 && !stream_eligible(g, s->L, s->S, s->S, form)) continue;
                 float t = INFINITY;
                 for (int r = 0; r < 4 && rc == PDFLOW_OK; ++r) {
                     cudaEventRecord(e0, s->stream);

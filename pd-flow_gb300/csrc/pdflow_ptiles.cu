@@ -22,7 +22,10 @@
 // results are bit-identical to every other iteration form.  Every pixel of
 // the region is updated in every iteration; the stale ring at non-border
 // region edges is never read by an exact pixel and only the interior is
-// stored.  Needs rows % 4 == 0 (16-byte aligned tensor-copy rows).
+// stored.  Needs rows % 4 == 0 (16-byte aligned tensor-copy rows); levels
+// with an even row count otherwise (a VGA solve's 30x40) run the tiles with
+// each thread loading its pixel pair's 32 values directly (8-byte loads, no
+// staging: such levels have about one region per CTA, nothing to stream).
 //
 // Strips (iteration form 10).  Of an iteration's column neighbours only the
 // primal step's backward difference looks left (ri * the dual's u-component
@@ -74,6 +77,7 @@ enum { S_DU, S_DV, S_DW, S_UA, S_VA, S_WA, S_PD, S_PUU, S_PUV, S_PVU, S_PVV, S_P
 
 struct StreamArgs {
     LevelGeom g;
+    const float* planes[32];   // direct loads: the 13 source state and 19 constant planes, in the staging order
     unsigned whole;            // strips: units 0 .. whole-1 are strips 0 .. whole-1
     unsigned tier_n[3], tier_p[3];   // strips: then tier i: tier_p[i] pieces of each of the next tier_n[i] strips
     unsigned* work;            // strips: [next unit - grid, CTAs finished], zero between launches
@@ -247,9 +251,10 @@ __device__ __forceinline__ void issue_region(const StreamArgs& a, const StreamMa
 // that the next region of the strip sees on its left
 constexpr int kCarryFloats = 2 * 4 * 3 * kSR;
 
-template <bool kStrips>
+template <bool kStrips, bool kTma = true>
 __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, const __grid_constant__ StreamMaps tm)
 {
+    static_assert(kTma || !kStrips, "the strips stream their regions");
     extern __shared__ __align__(128) float sm[];
     __shared__ __align__(8) unsigned long long bar_mem;
     __shared__ unsigned next_unit;   // strips: the unit thread 0 took for after the current one
@@ -269,7 +274,6 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
     float* YU = sm + Y_U * kSPlane;
     float* YV = sm + Y_V * kSPlane;
     float* YW = sm + Y_W * kSPlane;
-    auto ld2s = [&](int plane) { return *reinterpret_cast<const float2*>(sm + plane * kSPlane + me); };
 
     float* carry = sm + N_PLANES * kSPlane;
     const int cc = kSR - 1 - (int)a.kk;              // strips: the column the next region needs
@@ -280,7 +284,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
         tl = strip_at(a, blockIdx.x, -1, false);
     else
         tl = tile_at(a, blockIdx.x);
-    if (t == 0) {
+    if (kTma && t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (tl.more) issue_region(a, tm, sm, bar, tl);
@@ -295,7 +299,14 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
         const bool fv = (v0 == 0), lv = (v0 + 1 == R - 1);
         const bool last_launch = a.last || (pair_flags(a.g.map, tl.y) & kMapLast);
 
-        const bool ok = mbar_wait(bar, phase, kStreamWaitLimit);
+        const bool ok = kTma ? mbar_wait(bar, phase, kStreamWaitLimit) : true;
+        // the pair's value of plane k: from the staging copy, or loaded
+        // directly (zero outside the image, as the tensor copy fills)
+        auto ld2s = [&](int k) {
+            if constexpr (kTma) return *reinterpret_cast<const float2*>(sm + k * kSPlane + me);
+            return live ? __ldg(reinterpret_cast<const float2*>(at(a.planes[k], po) + v0 + (size_t)u * (size_t)R))
+                        : zero;
+        };
         float2 du = ld2s(S_DU), dv = ld2s(S_DV), dw = ld2s(S_DW), ua = ld2s(S_UA), va = ld2s(S_VA),
                wa = ld2s(S_WA), pd = ld2s(S_PD), puu = ld2s(S_PUU), puv = ld2s(S_PUV), pvu = ld2s(S_PVU),
                pvv = ld2s(S_PVV), pwu = ld2s(S_PWU), pwv = ld2s(S_PWV);
@@ -313,7 +324,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
             break;
         }
         phase ^= 1u;
-        if (t == 0) {
+        if (kTma && t == 0) {
             // the unit after this one (read by every thread after this tile's
             // iteration barriers; rewritten only after the next tile's first)
             unsigned unit = 0;
@@ -481,10 +492,34 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
 
 size_t stream_smem_bytes() { return sizeof(float) * (N_PLANES * kSPlane + kCarryFloats); }
 
+// The direct loads and stores move a pixel pair as one float2: even rows and
+// pair spacing, 8-byte aligned planes.
+bool stream_direct_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst)
+{
+    if (g.R % 2 != 0 || g.slots == 0 || g.pstride % 2 != 0) return false;
+    const float* cg[19] = {L.ri, L.rj, L.dct, L.dcu, L.dcv, L.ddt, L.ddu, L.ddv, L.mu, L.du_prev, L.dv_prev,
+                           L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4], L.qs[5], L.qs[6], L.qs[7]};
+    const float* sd[26] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd, src.puu, src.puv,
+                           src.pvu, src.pvv, src.pwu, src.pwv, dst.du, dst.dv, dst.dw, dst.dua, dst.dva,
+                           dst.dwa, dst.pd, dst.puu, dst.puv, dst.pvu, dst.pvv, dst.pwu, dst.pwv};
+    for (const float* q : cg)
+        if (!q || reinterpret_cast<uintptr_t>(q) % 8u != 0) return false;
+    for (const float* q : sd)
+        if (!q || reinterpret_cast<uintptr_t>(q) % 8u != 0) return false;
+    return true;
+}
+
+bool stream_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst, int form)
+{
+    if (quads_eligible(g, L, src, dst)) return true;
+    return (form == 8 || form == 9) && stream_direct_eligible(g, L, src, dst);
+}
+
 cudaError_t prepare_stream_tiles()
 {
     cudaError_t e = cudaSuccess;
-    for (const void* k : {(const void*)k_iterate_stream<false>, (const void*)k_iterate_stream<true>}) {
+    for (const void* k : {(const void*)k_iterate_stream<false>, (const void*)k_iterate_stream<true>,
+                          (const void*)k_iterate_stream<false, false>}) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stream_smem_bytes());
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -500,8 +535,12 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     // (16-byte tensor-copy coordinates): halo 4 (interior 24) or 8 (interior 16)
     const bool strips = layout == StreamLayout::Strips;
     const int kSH = layout == StreamLayout::Tiles16 ? 8 : 4, kST = kSR - 2 * kSH;
-    // same preconditions as the quad tiles (16-byte aligned planes, rows % 4 == 0)
-    if (kk == 0 || kk > (unsigned)kSH || !quads_eligible(g, L, src, dst) || !status || ctas == 0)
+    // the tensor copies need the quad tiles' preconditions (16-byte aligned
+    // planes at one spacing, rows % 4 == 0); the tiles also run on direct loads
+    // where the rows are even
+    const bool tma = quads_eligible(g, L, src, dst);
+    if (kk == 0 || kk > (unsigned)kSH || !status || ctas == 0 || reinterpret_cast<uintptr_t>(depth_old) % 8u != 0 ||
+        !(tma || (!strips && stream_direct_eligible(g, L, src, dst))))
         return cudaErrorInvalidValue;
     StreamArgs a;
     a.g = g;
@@ -543,8 +582,14 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
                            src.puu, src.puv, src.pvu, src.pvv, src.pwu, src.pwv};
     const float* cg[19] = {L.ri, L.rj, L.dct, L.dcu, L.dcv, L.ddt, L.ddu, L.ddv, L.mu, L.du_prev, L.dv_prev,
                            L.qs[0], L.qs[1], L.qs[2], L.qs[3], L.qs[4], L.qs[5], L.qs[6], L.qs[7]};
-    size_t ss = 0, cs = 0;
+    for (int k = 0; k < 13; ++k) a.planes[k] = sg[k];
+    for (int k = 0; k < 19; ++k) a.planes[13 + k] = cg[k];
     StreamMaps maps{};
+    if (!tma) {
+        k_iterate_stream<false, false><<<grid, kSThreads, stream_smem_bytes(), st>>>(a, maps);
+        return cudaGetLastError();
+    }
+    size_t ss = 0, cs = 0;
     if (!equally_spaced(sg, 13, &ss) || !equally_spaced(cg, 19, &cs) ||
         !encode_plane_group(&maps.state, sg[0], 13, ss, g.R, g.C, g.slots, g.pstride, kSR, kSR) ||
         !encode_plane_group(&maps.consts, cg[0], 19, cs, g.R, g.C, g.slots, g.pstride, kSR, kSR))

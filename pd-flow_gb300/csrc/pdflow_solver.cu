@@ -217,26 +217,29 @@ static bool level_runs_tiles(const pdflow_solver* s, const LevelGeom& g, unsigne
 // tiles (form 8), which deal fewer pixels to every SM, and levels whose 16x16
 // tiles all fit in one round of CTAs the deep tiles (form 9: twice the
 // iterations per launch where the launches are latency-bound, as the
-// autotuner finds for a single pair's 60x80 and 120x160 levels).
+// autotuner finds for a single pair's 60x80 and 120x160 levels).  Levels
+// whose rows are even but not a multiple of 4 (30x40) cannot run the strips'
+// tensor copies and take the same tile rule.
 static int level_form(const pdflow_solver* s, const LevelGeom& g, unsigned pairs, unsigned level)
 {
     const int forced = level < 8 ? s->level_form[level] : -1;
     if (forced >= 0) return forced;
-    if (s->iter_form == 10 && pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms))
+    if (s->iter_form == 10 && (pairs * ((g.R + 23u) / 24u) < unsigned(s->num_sms) ||
+                               !stream_eligible(g, s->L, s->S, s->S, 10)))
         return pairs * ((g.R + 15u) / 16u) * ((g.C + 15u) / 16u) <= unsigned(s->num_sms) ? 9 : 8;
     return s->iter_form;
 }
 
 // Whether level `level`'s tiles run register-resident (quad tiles, form 7, or
 // streamed tiles and strips, forms 8-10): chosen for the level and possible at its size
-// (rows % 4 == 0; other levels of such a solve run the paired 24x24 tiles,
-// form 5).
+// (rows % 4 == 0, or even rows for the streamed tiles; other levels of such a
+// solve run the paired 24x24 tiles, form 5).
 static bool level_runs_quads(const pdflow_solver* s, const LevelGeom& g, unsigned iters, unsigned pairs,
                              unsigned level)
 {
     if (!level_runs_tiles(s, g, iters, pairs, level)) return false;
     const int form = level_form(s, g, pairs, level);
-    return (form >= 7 && form <= 10) && quads_eligible(g, s->L, s->S, s->S);
+    return (form >= 7 && form <= 10) && stream_eligible(g, s->L, s->S, s->S, form);
 }
 
 // The step-size planes the level's set-up writes for its iteration form.

@@ -89,7 +89,7 @@ int pdflow_autotune(pdflow_solver* s, unsigned n, unsigned probe_iters, pdflow_t
         for (int c = 0; c < PDFLOW_TUNE_CANDIDATES; ++c) {
             rep.level[i].ms_per_iter[c] = NAN;
             if (kCandidates[c].form == 1 && !one_ok) continue;
-            if (kCandidates[c].form >= 7 && !quads_eligible(g, s->L, s->S, s->S)) continue;   // rows % 4 != 0
+            if (kCandidates[c].form >= 7 && !stream_eligible(g, s->L, s->S, s->S, kCandidates[c].form)) continue;
             s->level_form[i] = kCandidates[c].form;
             s->level_kk[i] = kCandidates[c].kk;
             float t = INFINITY;

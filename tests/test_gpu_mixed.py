@@ -51,8 +51,10 @@ def test_autotuned_mixed_batch_pairs_equal_single_solves(built_lib):
         assert (r["form"], r["iters_per_launch"]) in [(f, k) for f in (3, 4, 5, 6, 7, 8, 10) for k in (2, 3, 4)] + [
             (9, 4), (9, 6), (9, 8)]
         assert r["ms_per_iter"][0] is None                      # two kernels per iteration: not a mixed form
-        if r["step"] in ("15x20", "30x40"):
-            assert r["form"] <= 6                                # rows % 4 != 0: no register tiles
+        if r["step"] == "15x20":
+            assert r["form"] <= 6                                # odd rows: no register tiles
+        if r["step"] == "30x40":
+            assert r["form"] not in (7, 10)                      # rows % 4 != 0: no tensor-copy tiles
     for _ in range(2):                                           # graph capture, then replay
         b.solve()
         for k, r in enumerate(rows):
