@@ -21,6 +21,7 @@
 // Data written by another CTA is read with ld.global.cg (L2), never through a
 // possibly stale L1 line.  Per-pixel arithmetic is pdflow_math.cuh, identical
 // to the stage kernels, so the results are bit-for-bit the same.
+#include <algorithm>
 #include <atomic>
 
 #include <cooperative_groups.h>
@@ -35,6 +36,9 @@ namespace pdflow {
 namespace {
 
 constexpr unsigned kIterThreads = 1024;
+// One CTA owns a whole small level (at most 1200 pixels): fewer threads, so
+// that the level's plane pointers and per-pixel temporaries fit in registers.
+constexpr unsigned kSingleThreads = 384;
 constexpr unsigned long long kSpinLimit = 1ull << 24;   // ~seconds of polling, then give up
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
@@ -79,7 +83,7 @@ __device__ bool wait_neighbours(const IterArgs& a, unsigned need, unsigned long 
 enum { SDU, SDV, SDW, SUA, SVA, SWA, SPD, SPUU, SPUV, SPVU, SPVV, SPWU, SPWV, SNST };
 
 template <int kMode>
-__global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
+__global__ void __launch_bounds__(kMode == kIterSingle ? kSingleThreads : kIterThreads, 1) k_iterate(IterArgs a)
 {
     extern __shared__ float sm[];
     if (a.g.map || (kMode != kIterGrid && blockIdx.y > 0)) {
@@ -109,7 +113,9 @@ __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
     float* np = sm + SNST * ps;                   // 7 planes of new duals, [0, nsp)
     const LevelConsts& L = a.L;
     const float li = a.p.lambda_i, ld = a.p.lambda_d;
-    const bool has_left = (u0 > 0), has_right = (u1 < C);
+    // one CTA (kIterSingle) owns every column: no halo column, no neighbours
+    constexpr bool kOne = kMode == kIterSingle;
+    const bool has_left = !kOne && (u0 > 0), has_right = !kOne && (u1 < C);
 
     // initial state of the level (written by the set-up kernel into buffer 0)
     for (unsigned j = threadIdx.x; j < nown; j += blockDim.x) {
@@ -136,7 +142,7 @@ __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
         // ---- dual step over [h0, u1) ----
         for (unsigned j = threadIdx.x; j < nsp; j += blockDim.x) {
             const unsigned v = j % R, u = h0 + j / R, i = v + u * R;
-            const bool own = (u >= u0);
+            const bool own = kOne || (u >= u0);
             const unsigned jo = j - off;          // own-slab index (valid when own)
             const bool lu = (u == C - 1), lv = (v == R - 1);
             float dua, dva, dwa, dua_u, dva_u, dwa_u, dua_v, dva_v, dwa_v;
@@ -159,7 +165,7 @@ __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
             }
             if (lu) {
                 dua_u = dua; dva_u = dva; dwa_u = dwa;
-            } else if (u + 1 < u1) {
+            } else if (kOne || u + 1 < u1) {
                 const unsigned ju = (u + 1 - u0) * R + v;   // own column to the right
                 dua_u = st[SUA * ps + ju]; dva_u = st[SVA * ps + ju]; dwa_u = st[SWA * ps + ju];
             } else {
@@ -241,14 +247,14 @@ __global__ void __launch_bounds__(kIterThreads, 1) k_iterate(IterArgs a)
     // The duals go to buffer (iters & 1): the neighbours may still be reading
     // buffer ((iters - 1) & 1) in their last iteration, and nobody reads the
     // other one any more.
-    const int fb = a.iters & 1;
+    const bool fb = a.iters & 1;
     for (unsigned j = threadIdx.x; j < nown; j += blockDim.x) {
         const unsigned i = u0 * R + j;
         a.du[i] = st[SDU * ps + j];
         a.dv[i] = st[SDV * ps + j];
         a.dw[i] = st[SDW * ps + j];
 #pragma unroll
-        for (int k = 0; k < 7; ++k) a.p_[fb][k][i] = st[(SPD + k) * ps + j];
+        for (int k = 0; k < 7; ++k) (fb ? a.p_[1][k] : a.p_[0][k])[i] = st[(SPD + k) * ps + j];
     }
 }
 
@@ -359,7 +365,8 @@ cudaError_t launch_iterate(const IterPlan& pl, IterArgs a, cudaStream_t st)
     a.smem_state_plane = pl.smem_state_plane;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(pl.ctas, pl.mode == kIterGrid ? 1 : a.g.pairs);
-    cfg.blockDim = dim3(kIterThreads);
+    const unsigned single = std::min(kSingleThreads, (a.g.N + 31u) / 32u * 32u);
+    cfg.blockDim = dim3(pl.mode == kIterSingle ? single : kIterThreads);
     cfg.dynamicSmemBytes = pl.smem_bytes;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
