@@ -82,6 +82,98 @@ __device__ bool wait_neighbours(const IterArgs& a, unsigned need, unsigned long 
 //    7 planes of new duals over [h0, u1)
 enum { SDU, SDV, SDW, SUA, SVA, SWA, SPD, SPUU, SPUV, SPVU, SPVV, SPWU, SPWV, SNST };
 
+// A level with at most one pixel per thread of a single CTA: each thread
+// keeps its pixel's state, duals and constants in registers for all the
+// iterations, and only the values its neighbours read go through shared
+// memory (the over-relaxed primal for the forward differences of the right
+// and lower neighbours' duals; the TV duals for the backward divergence of
+// the left and upper ones).  The same per-pixel functions in the same order
+// as the general loop below, so the same bits.  Two barriers per iteration
+// order every exchange: a plane is rewritten only after the barrier that
+// follows its readers' last read.
+__device__ __forceinline__ void iterate_resident(const IterArgs& a, float* sm)
+{
+    const unsigned R = a.g.R, C = a.g.C, N = a.g.N;
+    const LevelConsts L = a.L;
+    const float li = a.p.lambda_i, ld = a.p.lambda_d;
+    float* xa = sm;                  // [3][N]: du_acc, dv_acc, dw_acc
+    float* xp = sm + 3 * N;          // [6][N]: puu, puv, pvu, pvv, pwu, pwv
+    const unsigned i = threadIdx.x;
+    const bool live = i < N;
+    const unsigned v = live ? i % R : 0, u = live ? i / R : 0;
+    const bool fu = (u == 0), lu = (u == C - 1), fv = (v == 0), lv = (v == R - 1);
+    const unsigned iu = lu ? i : i + R, iv = lv ? i : i + 1;   // right / lower neighbour (itself at a border)
+    const unsigned im = fu ? i : i - R, jm = fv ? i : i - 1;   // left / upper neighbour
+    float du = 0.f, dv = 0.f, dw = 0.f, ua = 0.f, va = 0.f, wa = 0.f;
+    Duals d{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float spd = 0.f, spuvx = 0.f, spuvy = 0.f, spwx = 0.f, spwy = 0.f, mu = 0.f, ddt = 0.f, ddu = 0.f, ddv = 0.f;
+    float ri = 0.f, rj = 0.f, ri_m = 0.f, rj_m = 0.f, dup = 0.f, dvp = 0.f, dup_u = 0.f, dvp_u = 0.f, dup_v = 0.f,
+          dvp_v = 0.f, tu = 0.f, tv = 0.f, tw = 0.f, dct = 0.f, dcu = 0.f, dcv = 0.f;
+    if (live) {
+        du = a.du[i];
+        dv = a.dv[i];
+        dw = a.dw[i];
+        ua = __ldcg(a.acc[0][0] + i);
+        va = __ldcg(a.acc[0][1] + i);
+        wa = __ldcg(a.acc[0][2] + i);
+        d = Duals{__ldcg(a.p_[0][0] + i), __ldcg(a.p_[0][1] + i), __ldcg(a.p_[0][2] + i), __ldcg(a.p_[0][3] + i),
+                  __ldcg(a.p_[0][4] + i), __ldcg(a.p_[0][5] + i), __ldcg(a.p_[0][6] + i)};
+        spd = __ldg(L.spd + i); spuvx = __ldg(L.spuvx + i); spuvy = __ldg(L.spuvy + i);
+        spwx = __ldg(L.spwx + i); spwy = __ldg(L.spwy + i); mu = __ldg(L.mu + i); ddt = __ldg(L.ddt + i);
+        ddu = __ldg(L.ddu + i); ddv = __ldg(L.ddv + i); ri = __ldg(L.ri + i); rj = __ldg(L.rj + i);
+        ri_m = fu ? ri : __ldg(L.ri + i - R);
+        rj_m = fv ? rj : __ldg(L.rj + i - 1);
+        dup = __ldg(L.du_prev + i); dvp = __ldg(L.dv_prev + i);
+        dup_u = __ldg(L.du_prev + iu); dvp_u = __ldg(L.dv_prev + iu);
+        dup_v = __ldg(L.du_prev + iv); dvp_v = __ldg(L.dv_prev + iv);
+        tu = __ldg(L.tu + i); tv = __ldg(L.tv + i); tw = __ldg(L.tw + i);
+        dct = __ldg(L.dct + i); dcu = __ldg(L.dcu + i); dcv = __ldg(L.dcv + i);
+    }
+    for (unsigned t = 0; t < a.iters; ++t) {
+        // ---- dual step ----
+        if (live) {
+            xa[i] = ua;
+            xa[N + i] = va;
+            xa[2 * N + i] = wa;
+        }
+        __syncthreads();
+        if (live) {
+            dual_update(d, spd, spuvx, spuvy, spwx, spwy, mu, ddt, ddu, ddv, li, ld, ri, rj, ua, va, wa, dup, dvp,
+                        xa[iu], xa[N + iu], xa[2 * N + iu], dup_u, dvp_u, xa[iv], xa[N + iv], xa[2 * N + iv], dup_v,
+                        dvp_v, lu, lv);
+            xp[i] = d.puu;
+            xp[N + i] = d.puv;
+            xp[2 * N + i] = d.pvu;
+            xp[3 * N + i] = d.pvv;
+            xp[4 * N + i] = d.pwu;
+            xp[5 * N + i] = d.pwv;
+        }
+        __syncthreads();
+        // ---- primal step ----
+        if (live) {
+            const float divu = divergence(ri, ri_m, rj, rj_m, d.puu, xp[im], d.puv, xp[N + jm], fu, lu, fv, lv);
+            const float divv = divergence(ri, ri_m, rj, rj_m, d.pvu, xp[2 * N + im], d.pvv, xp[3 * N + jm], fu, lu,
+                                          fv, lv);
+            const float divw = divergence(ri, ri_m, rj, rj_m, d.pwu, xp[4 * N + im], d.pwv, xp[5 * N + jm], fu, lu,
+                                          fv, lv);
+            primal_update(du, dv, dw, ua, va, wa, tu, tv, tw, mu, ddu, ddv, d.pd, li, ld, divu, divv, divw, dct, dcu,
+                          dcv);
+            if (t + 1 == a.iters) saturate(du, dv, dw, dup, dvp, __ldg(a.depth_old + i));
+        }
+    }
+    // final state for the weighted median, the duals to buffer (iters & 1),
+    // as the general loop leaves them
+    if (live) {
+        a.du[i] = du;
+        a.dv[i] = dv;
+        a.dw[i] = dw;
+        const bool fb = a.iters & 1;
+        const float pn[7] = {d.pd, d.puu, d.puv, d.pvu, d.pvv, d.pwu, d.pwv};
+#pragma unroll
+        for (int k = 0; k < 7; ++k) (fb ? a.p_[1][k] : a.p_[0][k])[i] = pn[k];
+    }
+}
+
 template <int kMode>
 __global__ void __launch_bounds__(kMode == kIterSingle ? kSingleThreads : kIterThreads, 1) k_iterate(IterArgs a)
 {
@@ -116,6 +208,10 @@ __global__ void __launch_bounds__(kMode == kIterSingle ? kSingleThreads : kIterT
     // one CTA (kIterSingle) owns every column: no halo column, no neighbours
     constexpr bool kOne = kMode == kIterSingle;
     const bool has_left = !kOne && (u0 > 0), has_right = !kOne && (u1 < C);
+    if (kOne && nsp <= blockDim.x) {
+        iterate_resident(a, sm);
+        return;
+    }
 
     // initial state of the level (written by the set-up kernel into buffer 0)
     for (unsigned j = threadIdx.x; j < nown; j += blockDim.x) {
