@@ -127,6 +127,27 @@ __device__ __forceinline__ void disc2(float2& a, float2& b)
     disc(a.y, b.y);
 }
 
+// shrink_rcp (pdflow_math.cuh) for both pixels of a pair: the quotients'
+// Markstein corrections and the three cases' values in packed FP32x2 (each
+// lane the same correctly rounded operations), the case chosen per lane.
+__device__ __forceinline__ float2 div_rcp2(float2 a, float2 b, float2 y)
+{
+    const float2 q0 = mul2(a, y);
+    const float2 q1 = fm2(fm2(neg2(q0), b, a), y, q0);
+    const float2 q2 = fm2(fm2(neg2(q1), b, a), y, q1);
+    return make_float2(a.x == 0.f ? a.x : q2.x, a.y == 0.f ? a.y : q2.y);
+}
+__device__ __forceinline__ void shrink_rcp2(float2& du, float2& dv, float2 of, float2 th, float2 den, float2 rden,
+                                            float2 a1, float2 b1)
+{
+    const float2 mu_ = sub2(du, div_rcp2(mul2(a1, of), den, rden));
+    const float2 mv_ = sub2(dv, div_rcp2(mul2(b1, of), den, rden));
+    const float2 pu = add2(du, a1), pv = add2(dv, b1), su = sub2(du, a1), sv = sub2(dv, b1);
+    const bool lox = of.x < -th.x, hix = of.x > th.x, loy = of.y < -th.y, hiy = of.y > th.y;
+    du = make_float2(lox ? pu.x : (hix ? su.x : mu_.x), loy ? pu.y : (hiy ? su.y : mu_.y));
+    dv = make_float2(lox ? pv.x : (hix ? sv.x : mv_.x), loy ? pv.y : (hiy ? sv.y : mv_.y));
+}
+
 // One region of a CTA's walk: its origin, the rows and columns it stores,
 // and (strips) where the walk goes next.
 struct Tile {
@@ -443,8 +464,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
                     const float2 of = fm2(dcv, dv, fm2(dcu, du, dct));
                     // quotients by the reciprocal when the whole warp is in its range
                     if (__all_sync(0xffffffffu, rcp_ok && shrink_rcp_ok(of.x) && shrink_rcp_ok(of.y))) {
-                        shrink_rcp(du.x, dv.x, of.x, th.x, den.x, rden.x, a1.x, b1.x);
-                        shrink_rcp(du.y, dv.y, of.y, th.y, den.y, rden.y, a1.y, b1.y);
+                        shrink_rcp2(du, dv, of, th, den, rden, a1, b1);
                     } else {
                         shrink(du.x, dv.x, of.x, th.x, a1.x, b1.x);
                         shrink(du.y, dv.y, of.y, th.y, a1.y, b1.y);
