@@ -650,8 +650,12 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
                 const int indr = (int)v + k, indc = (int)u + l;
                 const bool in = (indr >= 0) && (indr < (int)R) && (indc >= 0) && (indc < (int)C);
                 const int j = in ? (int)index + l * (int)R + k : (int)index;
-                wt[q] = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
-                               : median_weight(depth_old, o.dep[j], L.ddt[j]);
+                if (q == 4)   // the centre tap: z0 - z0
+                    wt[q] = qt(1.f, fm(10.f, kDdtSq ? L.spd[j] : powf(L.ddt[j], 2.f),
+                                       fm(5.f, pow2_diff_voted(depth_old, o.dep[j]), 1.f)));
+                else
+                    wt[q] = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
+                                   : median_weight(depth_old, o.dep[j], L.ddt[j]);
                 fu[q] = S.du[j];
                 fv[q] = S.dv[j];
                 fw[q] = S.dw[j];

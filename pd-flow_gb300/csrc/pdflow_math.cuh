@@ -379,6 +379,15 @@ __device__ __forceinline__ float median_weight_sq(float z0, float z, float ddt_s
     return qt(1.f, fm(10.f, ddt_sq, fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
 }
 
+// powf(z0 - z, 2.f) without the call where the difference is zero in every
+// active lane of the warp (the centre tap): powf(+-0, 2) is +0.
+__device__ __forceinline__ float pow2_diff_voted(float z0, float z)
+{
+    const float d = sub(z0, z);
+    if (__all_sync(__activemask(), d == 0.f)) return 0.f;
+    return powf(d, 2.f);
+}
+
 // Linear interpolation between the samples bracketing the weighted median
 // (pdflow_cudalib.cu:1109).
 __device__ __forceinline__ float median_lerp(float cum_r, float cum_l, float med, float f_l, float f_r)
