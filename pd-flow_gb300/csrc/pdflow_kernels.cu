@@ -565,7 +565,7 @@ __global__ void k_saturate(LevelGeom g, LevelConsts L, State S, const float* dep
 // reference does, and the bracketing samples are interpolated; the result and
 // the selected index are the reference's bit for bit.  Every index is a
 // compile-time constant: nothing spills.
-__device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned present, unsigned n,
+__device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9], unsigned present,
                                          float med_or_neg, float* total, int32_t* cont_out)
 {
     // the samples in tap order, a missing one (bit clear in `present`) as +inf
@@ -593,27 +593,36 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
             sf[a + 1] = sw_ ? tf : sf[a + 1];
             sw[a + 1] = sw_ ? tw : sw[a + 1];
         }
+    // cumulative weights; the missing samples (weight +0, sorted last) leave
+    // the sum as it is (x + 0 == x for the non-negative sums), so cum[8] is
+    // the reference's cum[n - 1]
     float cum[9];
     cum[0] = sw[0];
 #pragma unroll
-    for (int r = 1; r < 9; ++r) cum[r] = ((unsigned)r < n) ? add(cum[r - 1], sw[r]) : cum[r - 1];
-    *total = cum[8];   // == cum[n-1]
+    for (int r = 1; r < 9; ++r) cum[r] = add(cum[r - 1], sw[r]);
+    *total = cum[8];
     const float med = (med_or_neg < 0.f) ? mul(0.5f, cum[8]) : med_or_neg;
+    // the reference counts the samples with med > cum (among the present
+    // ones: a missing one's cum is the total, never below med) and
+    // interpolates between that sample and the one before; cum does not
+    // decrease, so the counted samples are a prefix and one pass finds both
     int cont = 0;
-#pragma unroll
-    for (int r = 0; r < 9; ++r)
-        if ((unsigned)r < n && med > cum[r]) ++cont;
-    *cont_out = cont;
-    if (cont == 0) return sf[0];
     float cr = 0.f, cl = 0.f, fr = 0.f, fl = 0.f;
 #pragma unroll
-    for (int r = 1; r < 9; ++r)
-        if (r == cont) {
-            cr = cum[r];
-            cl = cum[r - 1];
-            fr = sf[r];
-            fl = sf[r - 1];
-        }
+    for (int r = 0; r < 8; ++r) {
+        const bool t = med > cum[r];
+        cont = t ? r + 1 : cont;
+        cl = t ? cum[r] : cl;
+        fl = t ? sf[r] : fl;
+        cr = t ? cum[r + 1] : cr;
+        fr = t ? sf[r + 1] : fr;
+    }
+    if (med > cum[8]) {   // past every sample: the reference finds no bracket
+        cont = 9;
+        cr = cl = fr = fl = 0.f;
+    }
+    *cont_out = cont;
+    if (cont == 0) return sf[0];
     return median_lerp(cr, cl, med, fl, fr);
 }
 
@@ -651,8 +660,8 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
                 const bool in = (indr >= 0) && (indr < (int)R) && (indc >= 0) && (indc < (int)C);
                 const int j = in ? (int)index + l * (int)R + k : (int)index;
                 if (q == 4)   // the centre tap: z0 - z0
-                    wt[q] = qt(1.f, fm(10.f, kDdtSq ? L.spd[j] : powf(L.ddt[j], 2.f),
-                                       fm(5.f, pow2_diff_voted(depth_old, o.dep[j]), 1.f)));
+                    wt[q] = __frcp_rn(fm(10.f, kDdtSq ? L.spd[j] : powf(L.ddt[j], 2.f),
+                                         fm(5.f, pow2_diff_voted(depth_old, o.dep[j]), 1.f)));
                 else
                     wt[q] = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
                                    : median_weight(depth_old, o.dep[j], L.ddt[j]);
@@ -661,13 +670,12 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
                 fw[q] = S.dw[j];
                 present |= (in ? 1u : 0u) << q;
             }
-        const unsigned n = __popc(present);
         float tot;
         int32_t c0, c1, c2;
-        ru = median9(fu, wt, present, n, -1.f, &tot, &c0);
+        ru = median9(fu, wt, present, -1.f, &tot, &c0);
         const float pres_med = mul(0.5f, tot);   // half of u's total, for all three (:1097)
-        rv = median9(fv, wt, present, n, pres_med, &tot, &c1);
-        rw = median9(fw, wt, present, n, pres_med, &tot, &c2);
+        rv = median9(fv, wt, present, pres_med, &tot, &c1);
+        rw = median9(fw, wt, present, pres_med, &tot, &c2);
         if (sel) { sel[index] = c0; sel[g.N + index] = c1; sel[2 * g.N + index] = c2; }
     } else {
         ru = S.du[index];

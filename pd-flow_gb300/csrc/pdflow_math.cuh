@@ -370,13 +370,13 @@ __device__ __forceinline__ void saturate(float& du, float& dv, float& dw, float 
 // 1 / (1 + 5 (z0 - z)^2 + 10 ddt^2).
 __device__ __forceinline__ float median_weight(float z0, float z, float ddt)
 {
-    return qt(1.f, fm(10.f, powf(ddt, 2.f), fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
+    return __frcp_rn(fm(10.f, powf(ddt, 2.f), fm(5.f, powf(sub(z0, z), 2.f), 1.f)));   // 1 / x, IEEE rounded
 }
 
 // The same weight from a precomputed ddt_sq = powf(ddt, 2.f).
 __device__ __forceinline__ float median_weight_sq(float z0, float z, float ddt_sq)
 {
-    return qt(1.f, fm(10.f, ddt_sq, fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
+    return __frcp_rn(fm(10.f, ddt_sq, fm(5.f, powf(sub(z0, z), 2.f), 1.f)));
 }
 
 // powf(z0 - z, 2.f) without the call where the difference is zero in every
