@@ -578,13 +578,18 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
     a.total = a.tiles * g.pairs;
     const unsigned grid = ctas < a.total ? ctas : a.total;
-    // strip units: the last grid / 4 strips in 8 pieces, the grid / 2 before
-    // them in 4, the grid before those in 2, the rest whole; no more strips
-    // than CTAs: every strip in as many pieces as CTAs allow.  Pieces are at
-    // least one restart region's 32 - 2 kk exact columns wide.
+    // strip units: the last grid / 8 strips in 8 pieces (grid / 4 for strips
+    // of 16 regions or more), the grid / 8 before them in 4, the grid / 8
+    // before those in 2, the rest whole; no more strips than CTAs: every
+    // strip in as many pieces as CTAs allow.  Pieces are at least one restart
+    // region's 32 - 2 kk exact columns wide.  Each piece recomputes a left
+    // halo, so the tail is kept short: on 64-pair VGA solves (1 280 strips of
+    // 23 regions at 480x640, 640 of 12 at 240x320) the last grid / 4, grid / 2
+    // and grid strips in 8, 4 and 2 pieces took 38.06 ms, these tiers 37.3 ms.
     const unsigned strips_n = g.pairs * a.tiles_v, most = (g.C + (kSR - 2 * kk) - 1) / (kSR - 2 * kk);
+    const unsigned regions = (g.C + (kSR - kk) - 1) / (kSR - kk);   // of a whole strip walked with the carry
     unsigned left = strips_n;
-    const unsigned tn[3] = {grid, grid / 2, grid / 4}, tp[3] = {2, 4, 8};
+    const unsigned tn[3] = {grid / 8, grid / 8, regions >= 16 ? grid / 4 : grid / 8}, tp[3] = {2, 4, 8};
     for (int i = 2; i >= 0; --i) {
         a.tier_n[i] = strips_n > grid ? std::min(tn[i], left) : 0u;
         a.tier_p[i] = std::min(tp[i], most);
