@@ -232,11 +232,13 @@ int pdflow_read_flow_mixed(pdflow_solver* s, unsigned k, float* dx, float* dy, f
  * 24x24 tiles with the state in registers, 256 threads owning four rows each,
  * two CTAs per SM, levels with rows % 4 == 0; form 8: the same regions
  * walked by one persistent CTA per SM with the state and constants in
- * registers while the next region streams into shared memory by TMA, levels
- * with rows % 4 == 0; form 9: the same with 16x16 interiors and a halo of 8,
+ * registers while the next region streams into shared memory by TMA (levels
+ * with rows % 4 == 0; other even row counts load each pixel pair directly);
+ * form 9: the same with 16x16 interiors and a halo of 8,
  * up to 8 iterations per launch, for levels whose launches are latency-bound;
  * form 10: rows of regions walked left to right, each handing the next its
- * last exact column's exchange values, so no left halo is recomputed).
+ * last exact column's exchange values, so no left halo is recomputed; levels
+ * with rows % 4 == 0).
  * pdflow_autotune times every eligible candidate of every
  * level for pairs [0, n) of the pushed frames (probe_iters iterations each,
  * 0 = 12; use a multiple of 12 so every candidate runs whole launches) and keeps the fastest per level; all forms give the same bits.  The

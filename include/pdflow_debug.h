@@ -39,7 +39,8 @@ int pdflow_debug_solve(pdflow_solver* s, pdflow_dump_fn fn, void* ctx);
  * constants in registers (one pixel pair per thread, packed FP32x2) while
  * the next tile's region streams into shared memory by two 4D TMA tensor
  * copies; levels whose row count is even but not a multiple of 4 (30x40)
- * load each pixel pair directly instead, and 15x20 runs form 5 there; 7 = the same tiles as one CTA per tile, four rows per
+ * load each pixel pair directly instead, and 15x20 runs form 5 there;
+ * 7 = the same tiles as one CTA per tile, four rows per
  * thread with the state in registers and the constants in shared memory;
  * 5 = every level of a batch, and a single pair's levels above
  * 300 pixels (all but 15x20), as temporally blocked shared-memory tiles (several
