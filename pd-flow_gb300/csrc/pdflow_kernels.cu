@@ -626,12 +626,24 @@ __device__ __forceinline__ float median9(const float (&f)[9], const float (&w)[9
     return median_lerp(cr, cl, med, fl, fr);
 }
 
+// The median's pixels in tiles of kMedRows x kMedCols (rows along
+// threadIdx.x, so a warp's loads are one column's consecutive rows): the
+// block first stages its tile and a one-pixel halo of the five planes the
+// taps read, then every pixel takes its nine taps from shared memory at
+// fixed offsets (outside the image the halo holds zeros; those taps are
+// missing in `present` and never reach the median).
+constexpr int kMedRows = 32, kMedCols = 8;
+constexpr int kMedHR = kMedRows + 2, kMedHC = kMedCols + 2;
+
 template <bool kDdtSq>   // L.spd holds powf(ddt, 2) (levels run as tiles)
-__global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, State S, State Salt, LevelSol out,
-                         float* dx, float* dy, float* dz, Params p, int32_t* sel)
+__global__ void __launch_bounds__(kMedRows * kMedCols) k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L,
+                                                               State S, State Salt, LevelSol out, float* dx,
+                                                               float* dy, float* dz, Params p, int32_t* sel)
 {
-    const size_t po = pair_off(g.map, g.pstride, blockIdx.y);
-    const unsigned pf = pair_flags(g.map, blockIdx.y);
+    __shared__ float t_dep[kMedHC][kMedHR], t_sq[kMedHC][kMedHR], t_du[kMedHC][kMedHR], t_dv[kMedHC][kMedHR],
+        t_dw[kMedHC][kMedHR];
+    const size_t po = pair_off(g.map, g.pstride, blockIdx.z);
+    const unsigned pf = pair_flags(g.map, blockIdx.z);
     finest = finest || (pf & kMapFinest);
     o = at(o, po);
     L = at(L, po);
@@ -640,35 +652,54 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
     dx = at(dx, po);
     dy = at(dy, po);
     dz = at(dz, po);
-    const unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
-    if (index >= g.N) return;
-    const unsigned R = g.R, C = g.C;
-    const unsigned v = index % R, u = index / R;
-    const float depth_old = o.dep[index];
+    const int R = (int)g.R, C = (int)g.C;
+    const int v0 = (int)blockIdx.x * kMedRows, u0 = (int)blockIdx.y * kMedCols;
+    // the tile and its halo: rows v0-1 .. v0+kMedRows, columns u0-1 .. u0+kMedCols
+    for (int e = threadIdx.y * kMedRows + threadIdx.x; e < kMedHR * kMedHC; e += kMedRows * kMedCols) {
+        const int hr = e % kMedHR, hc = e / kMedHR, gv = v0 - 1 + hr, gu = u0 - 1 + hc;
+        float z = 0.f, q = 0.f, a = 0.f, b = 0.f, c = 0.f;
+        if (gv >= 0 && gv < R && gu >= 0 && gu < C) {
+            const int j = gv + gu * R;
+            z = o.dep[j];
+            q = kDdtSq ? L.spd[j] : powf(L.ddt[j], 2.f);
+            a = S.du[j];
+            b = S.dv[j];
+            c = S.dw[j];
+        }
+        t_dep[hc][hr] = z;
+        t_sq[hc][hr] = q;
+        t_du[hc][hr] = a;
+        t_dv[hc][hr] = b;
+        t_dw[hc][hr] = c;
+    }
+    __syncthreads();
+    const int tv = (int)threadIdx.x, tu = (int)threadIdx.y;
+    const int v = v0 + tv, u = u0 + tu;
+    if (v >= R || u >= C) return;
+    const unsigned index = (unsigned)(v + u * R);
+    const float depth_old = t_dep[tu + 1][tv + 1];
     float ru, rv, rw;
     if (depth_old > 0.f) {
         // the nine taps in the reference's order (row offset, then column);
         // taps outside the image are marked missing (median9)
+        unsigned present = 0x1ffu;
+        if (v == 0) present &= ~0x007u;       // row offset -1: taps 0, 1, 2
+        if (v == R - 1) present &= ~0x1c0u;   // row offset +1: taps 6, 7, 8
+        if (u == 0) present &= ~0x049u;       // column offset -1: taps 0, 3, 6
+        if (u == C - 1) present &= ~0x124u;   // column offset +1: taps 2, 5, 8
         float fu[9], fv[9], fw[9], wt[9];
-        unsigned present = 0;
 #pragma unroll
         for (int k = -1; k < 2; k++)
 #pragma unroll
             for (int l = -1; l < 2; l++) {
                 const int q = 3 * (k + 1) + (l + 1);
-                const int indr = (int)v + k, indc = (int)u + l;
-                const bool in = (indr >= 0) && (indr < (int)R) && (indc >= 0) && (indc < (int)C);
-                const int j = in ? (int)index + l * (int)R + k : (int)index;
-                if (q == 4)   // the centre tap: z0 - z0
-                    wt[q] = __frcp_rn(fm(10.f, kDdtSq ? L.spd[j] : powf(L.ddt[j], 2.f),
-                                         fm(5.f, pow2_diff_voted(depth_old, o.dep[j]), 1.f)));
-                else
-                    wt[q] = kDdtSq ? median_weight_sq(depth_old, o.dep[j], L.spd[j])
-                                   : median_weight(depth_old, o.dep[j], L.ddt[j]);
-                fu[q] = S.du[j];
-                fv[q] = S.dv[j];
-                fw[q] = S.dw[j];
-                present |= (in ? 1u : 0u) << q;
+                const int hc = tu + 1 + l, hr = tv + 1 + k;
+                const float dz2 = (q == 4) ? pow2_diff_voted(depth_old, t_dep[hc][hr])   // the centre: z0 - z0
+                                           : powf(sub(depth_old, t_dep[hc][hr]), 2.f);
+                wt[q] = __frcp_rn(fm(10.f, t_sq[hc][hr], fm(5.f, dz2, 1.f)));
+                fu[q] = t_du[hc][hr];
+                fv[q] = t_dv[hc][hr];
+                fw[q] = t_dw[hc][hr];
             }
         float tot;
         int32_t c0, c1, c2;
@@ -678,9 +709,9 @@ __global__ void k_median(LevelGeom g, bool finest, PyrLevel o, LevelConsts L, St
         rw = median9(fw, wt, present, pres_med, &tot, &c2);
         if (sel) { sel[index] = c0; sel[g.N + index] = c1; sel[2 * g.N + index] = c2; }
     } else {
-        ru = S.du[index];
-        rv = S.dv[index];
-        rw = S.dw[index];
+        ru = t_du[tu + 1][tv + 1];
+        rv = t_dv[tu + 1][tv + 1];
+        rw = t_dw[tu + 1][tv + 1];
         if (sel) { sel[index] = -1; sel[g.N + index] = -1; sel[2 * g.N + index] = -1; }
     }
     out.du[index] = ru;
@@ -908,11 +939,12 @@ cudaError_t launch_median(LevelGeom g, bool finest, PyrLevel old_l, LevelConsts 
                           float* dy, float* dz, Params p, int32_t* sel, cudaStream_t st, const State* alt,
                           bool ddt_sq)
 {
+    const dim3 grid((g.R + kMedRows - 1) / kMedRows, (g.C + kMedCols - 1) / kMedCols, g.pairs);
+    const dim3 block(kMedRows, kMedCols);
     if (ddt_sq)
-        k_median<true><<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p, sel);
+        k_median<true><<<grid, block, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p, sel);
     else
-        k_median<false><<<level_grid(g), kBlock, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p,
-                                                          sel);
+        k_median<false><<<grid, block, 0, st>>>(g, finest, old_l, L, S, alt ? *alt : S, out, dx, dy, dz, p, sel);
     return cudaGetLastError();
 }
 
