@@ -113,6 +113,15 @@ int pdflow_set_quad_prefetch(unsigned ctas_ahead);
  * use it in and returns how many differ (0 expected). */
 int pdflow_check_div_rcp(unsigned long long pairs, unsigned long long seed, unsigned long long* mismatches);
 
+/* The strip walk's work units (iteration form 10; no counterpart in the
+ * reference), as the launcher computes them for `bands` 24-row bands of
+ * `cols` columns on `ctas` CTAs at `iters_per_launch` iterations per launch:
+ * bands [0, *whole) are whole units, then for tier i = 0, 1, 2 the next
+ * tier_n[i] bands are cut into tier_p[i] column pieces each (host
+ * arithmetic only, no GPU needed). */
+int pdflow_strip_units(unsigned bands, unsigned cols, unsigned iters_per_launch, unsigned ctas, unsigned* whole,
+                       unsigned* tier_n, unsigned* tier_p);
+
 /* Copy bandwidth of this GPU for a working set of `bytes` per buffer (the
  * roofline denominators; no counterpart in the reference): allocates two
  * buffers of `bytes` and copies them into each other `reps` times within one

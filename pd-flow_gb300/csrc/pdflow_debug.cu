@@ -9,6 +9,7 @@
 #include "../../include/pdflow.h"
 #include "../../include/pdflow_debug.h"
 #include "pdflow_internal.h"
+#include "pdflow_iterate.cuh"
 #include "pdflow_kernels.cuh"
 #include "pdflow_math.cuh"
 
@@ -315,6 +316,21 @@ int pdflow_check_div_rcp(unsigned long long pairs, unsigned long long seed, unsi
     if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost);
     cudaFree(d);
     return e == cudaSuccess ? PDFLOW_OK : fail("division check", e);
+}
+
+int pdflow_strip_units(unsigned bands, unsigned cols, unsigned iters_per_launch, unsigned ctas, unsigned* whole,
+                       unsigned* tier_n, unsigned* tier_p)
+{
+    if (!whole || !tier_n || !tier_p) return fail(PDFLOW_ERR_ARG, "null output");
+    if (bands == 0 || cols == 0 || ctas == 0 || iters_per_launch == 0 || iters_per_launch > 4)
+        return fail(PDFLOW_ERR_ARG, "bands, columns and CTAs must be positive, 1 <= iterations per launch <= 4");
+    const pdflow::StripUnits su = pdflow::strip_units(bands, cols, iters_per_launch, ctas);
+    *whole = su.whole;
+    for (int i = 0; i < 3; ++i) {
+        tier_n[i] = su.tier_n[i];
+        tier_p[i] = su.tier_p[i];
+    }
+    return PDFLOW_OK;
 }
 
 int pdflow_measure_copy_gbs(size_t bytes, unsigned reps, void* stream, float* gbs)

@@ -77,6 +77,13 @@ enum class StreamLayout { Tiles24, Tiles16, Strips };
 // streamed tiles (8, 9) also run on direct loads where the rows are even.
 bool stream_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst, int form);
 bool stream_direct_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst);
+// The strip walk's units for `strips_n` bands of C columns on `grid` CTAs at
+// kk iterations per launch: bands [0, whole) whole, then for tier i = 0..2
+// the next tier_n[i] bands in tier_p[i] column pieces each.
+struct StripUnits {
+    unsigned whole, tier_n[3], tier_p[3];
+};
+StripUnits strip_units(unsigned strips_n, unsigned C, unsigned kk, unsigned grid);
 inline StreamLayout stream_layout(int form)
 {
     return form == 9 ? StreamLayout::Tiles16 : (form == 10 ? StreamLayout::Strips : StreamLayout::Tiles24);

@@ -512,6 +512,36 @@ __global__ void __launch_bounds__(kSThreads, 1) k_iterate_stream(StreamArgs a, c
 
 size_t stream_smem_bytes() { return sizeof(float) * (N_PLANES * kSPlane + kCarryFloats); }
 
+// Strip units: the last grid / 8 strips in 8 pieces (grid / 4 for strips
+// of 16 regions or more), the grid / 8 before them in 4, the grid / 8 before
+// those in 2, the rest whole; no more strips than CTAs: every strip in as
+// many pieces as CTAs allow.  Pieces are at least one restart region's
+// 32 - 2 kk exact columns wide.  Each piece recomputes a left halo, so the
+// tail is kept short: on 64-pair VGA solves (1 280 strips of 23 regions at
+// 480x640, 640 of 12 at 240x320) the last grid / 4, grid / 2 and grid strips
+// in 8, 4 and 2 pieces took 38.06 ms, these tiers 37.3 ms.
+StripUnits strip_units(unsigned strips_n, unsigned C, unsigned kk, unsigned grid)
+{
+    StripUnits su{};
+    if (strips_n == 0 || C == 0 || kk == 0 || 2 * kk >= (unsigned)kSR || grid == 0) return su;
+    const unsigned most = (C + (kSR - 2 * kk) - 1) / (kSR - 2 * kk);
+    const unsigned regions = (C + (kSR - kk) - 1) / (kSR - kk);   // of a whole strip walked with the carry
+    unsigned left = strips_n;
+    const unsigned tn[3] = {grid / 8, grid / 8, regions >= 16 ? grid / 4 : grid / 8}, tp[3] = {2, 4, 8};
+    for (int i = 2; i >= 0; --i) {
+        su.tier_n[i] = strips_n > grid ? std::min(tn[i], left) : 0u;
+        su.tier_p[i] = std::min(tp[i], most);
+        left -= su.tier_n[i];
+    }
+    if (strips_n <= grid) {
+        su.tier_n[0] = strips_n;
+        su.tier_p[0] = std::max(1u, std::min(grid / strips_n, most));
+        left = 0;
+    }
+    su.whole = left;
+    return su;
+}
+
 // The direct loads and stores move a pixel pair as one float2: even rows and
 // pair spacing, 8-byte aligned planes.
 bool stream_direct_eligible(const LevelGeom& g, const LevelConsts& L, const State& src, const State& dst)
@@ -578,29 +608,12 @@ cudaError_t launch_iterate_stream(LevelGeom g, LevelConsts L, State src, State d
     a.tiles = a.tiles_v * ((g.C + kST - 1) / kST);
     a.total = a.tiles * g.pairs;
     const unsigned grid = ctas < a.total ? ctas : a.total;
-    // strip units: the last grid / 8 strips in 8 pieces (grid / 4 for strips
-    // of 16 regions or more), the grid / 8 before them in 4, the grid / 8
-    // before those in 2, the rest whole; no more strips than CTAs: every
-    // strip in as many pieces as CTAs allow.  Pieces are at least one restart
-    // region's 32 - 2 kk exact columns wide.  Each piece recomputes a left
-    // halo, so the tail is kept short: on 64-pair VGA solves (1 280 strips of
-    // 23 regions at 480x640, 640 of 12 at 240x320) the last grid / 4, grid / 2
-    // and grid strips in 8, 4 and 2 pieces took 38.06 ms, these tiers 37.3 ms.
-    const unsigned strips_n = g.pairs * a.tiles_v, most = (g.C + (kSR - 2 * kk) - 1) / (kSR - 2 * kk);
-    const unsigned regions = (g.C + (kSR - kk) - 1) / (kSR - kk);   // of a whole strip walked with the carry
-    unsigned left = strips_n;
-    const unsigned tn[3] = {grid / 8, grid / 8, regions >= 16 ? grid / 4 : grid / 8}, tp[3] = {2, 4, 8};
-    for (int i = 2; i >= 0; --i) {
-        a.tier_n[i] = strips_n > grid ? std::min(tn[i], left) : 0u;
-        a.tier_p[i] = std::min(tp[i], most);
-        left -= a.tier_n[i];
+    const StripUnits su = strip_units(g.pairs * a.tiles_v, g.C, kk, grid);
+    a.whole = su.whole;
+    for (int i = 0; i < 3; ++i) {
+        a.tier_n[i] = su.tier_n[i];
+        a.tier_p[i] = su.tier_p[i];
     }
-    if (strips_n <= grid) {
-        a.tier_n[0] = strips_n;
-        a.tier_p[0] = std::max(1u, std::min(grid / strips_n, most));
-        left = 0;
-    }
-    a.whole = left;
     a.work = status + 2;
     // the runs of planes (quads_eligible checked that each is equally spaced)
     const float* sg[13] = {src.du, src.dv, src.dw, src.dua, src.dva, src.dwa, src.pd,

@@ -195,6 +195,8 @@ _SIGNATURES = {
     "pdflow_set_quad_prefetch": (ctypes.c_int, [ctypes.c_uint]),
     "pdflow_measure_copy_gbs": (ctypes.c_int, [ctypes.c_size_t, u32, vp, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_check_div_rcp": (ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "pdflow_strip_units": (ctypes.c_int, [u32, u32, u32, u32, ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                          ctypes.POINTER(u32)]),
     "pdflow_debug_wait_timeout": (ctypes.c_int, [vp, u32]),
     "pdflow_trace_solve": (ctypes.c_int, [vp, u32, ctypes.POINTER(ctypes.c_float)]),
     "pdflow_create_mixed": (ctypes.c_int, [u32, ctypes.POINTER(vp)]),
